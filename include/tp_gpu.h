@@ -1,0 +1,228 @@
+/*
+ * tp_gpu.h -- C ABI of libtpgpu.so, the GB300 (sm_103a) test-particle tracer.
+ *
+ * Part 1 re-exports, with the same names and signatures, the entry points of
+ * the reference C API on the tracking hot path, so that the reference's own
+ * callers (main.c, test_particle.c, domain.c, diagnostics.c, ...) link
+ * against this library instead of tracking.o / emfields.o / interpolation.o /
+ * force_free.o / wlcs.o and the field modules.  Every compute entry point runs
+ * on the GPU; there is no CPU path.  Errors follow the reference: a message on
+ * stdout and exit(1); tp_last_status()/tp_last_error() report the cause.
+ *
+ * Part 2 is this library's own API (tp_*): device-resident sessions, batch
+ * utilities and the precision / mode switches used by the tests and benchmark.
+ *
+ * Reference locations are paths inside the reference project.
+ */
+#ifndef TP_GPU_H
+#define TP_GPU_H
+#include "tp_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ======================================================================
+ * Part 1: reference-compatible entry points
+ * ==================================================================== */
+
+/* --- tracking (include/tracking.h:22-85, src/tracking.c) --- */
+/* src/tracking.c:53-59 */
+void set_variables_tracking(grids *sgrid, domain *sdomain, int stype, int mt);
+/* src/tracking.c:61-65 */
+void set_ptl_params_tracking(int pbc, double qm);
+/* src/tracking.c:659-699: fixed-step tracking of all particles on the GPU; appends
+ * nt_out spectra to data/espectrum.dat (and data/espect_escape.dat when bc_flag
+ * is 1) and writes data/diff_coeffs.dat through collect_espectrum /
+ * collect_diff_coeffs, which the caller's diagnostics.c provides.
+ * tracking_method 1 runs the adaptive Bulirsch-Stoer stepper (the reference's
+ * adaptive branch, src/tracking.c:681-684, is commented out). */
+void particle_tracking_hybrid(int mpi_rank, int nptl, double dt, int nbins,
+        int nt_out, int bc_flag, int nsteps_output, double pmass,
+        int *ntraj_accum, int tracking_method, int traj_diagnose,
+        particles *ptl_init, int *nsteps_ptl_tracking, particles *ptl,
+        particles *ptl_time);
+/* src/tracking.c:90-190.  The spectrum arguments are the reference's
+ * double[nt_out][nbins] / double[threads+1][nbins*nt_out] arrays. */
+void particle_tracking_fixed_time_step(int mpi_rank, int nptl, double dt,
+        int nbins, int nt_out, int traj_diagnose, int nsteps_output, double pmass,
+        int *ntraj_accum, particles *ptl_init, int *nsteps_ptl_tracking, particles *ptl,
+        double *espectrum, double *espect_tot, double *espect_escape,
+        double *espect_private, double *espect_escape_private, particles *ptl_time);
+/* src/tracking.c:297-374: steps sstep..estep of all particles; spectra go to
+ * row tid of espect_private, diffusion sums are added to drr..dee. */
+void particle_tracking_multi_steps_openmp(int nptl, double dt, int tid, int sstep,
+        int estep, int nbins, int nt_out, int einterval_t, int traj_diagnose,
+        int nsteps_output, double pmass, int *ntraj_accum, particles *ptl_init,
+        int *ntraj_diagnostics_points_array, particles *ptl,
+        int *nsteps_ptl_tracking, double *espect_private,
+        double *espect_escape_private, particles *ptl_time,
+        int *nptl_remain_time, double *drr, double *dxx, double *dyy, double *dzz,
+        double *dpp, double *duu, double *daa, double *dee);
+/* src/tracking.c:416-462: one step of one particle */
+void particle_tracking_single_step_openmp(int iptl, int it, double dt, int tid,
+        int einterval_t, int traj_diagnose, int nbins, int nt_out, int nsteps_output,
+        double pmass, particles *ptl_init, int ntraj_offset_local, int *ntp, particles *ptl,
+        int *iescape_pre, int *iescape_after, int *ntraj_diagnostics_points,
+        int *nsteps_ptl_tracking, double *espect_private,
+        double *espect_escape_private, particles *ptl_time,
+        double *drr, double *dxx, double *dyy, double *dzz, double *dpp,
+        double *duu, double *daa, double *dee);
+/* src/tracking.c:475-493 */
+void gather_particle_spectra_openmp(int num_threads, int nbins, int nt_out,
+        double *espectrum, double *espect_private,
+        double *espect_escape, double *espect_escape_private);
+/* src/tracking.c:749-892: one Wirz push of one particle */
+void tracking_wirz(struct particles *ptl, double dt);
+/* src/tracking.c:1172-1221 */
+void particle_bc(particles *ptl, int *iescape);
+/* src/tracking.c:1226-1255: parses init.dat */
+double get_tracking_time_interval(int mpi_rank, char *config_file_name, double pmass);
+/* src/tracking.c:1084-1140: scalar helpers of the reference API */
+void cross_product(double beta_x, double beta_y, double beta_z, double Bx,
+        double By, double Bz, double *Cx, double *Cy, double *Cz);
+double getgamma(double dx, double dy, double dz);
+void getdelta(double *delta_x, double *delta_y, double *delta_z,
+        double beta_x, double beta_y, double beta_z);
+double modulus(double x, double y, double z);
+
+/* --- fields (include/emfields.h:28-40, src/emfields.c) --- */
+void get_emf(double x, double y, double z, double t, struct emfields *emf);            /* :32-60 */
+void get_magnetic_field(double x, double y, double z, double t, struct emfields *emf); /* :76-96 */
+void set_variables_emfields(int stype);                                                 /* :196-199 */
+void getemf_test(double x, double y, double z, double t, struct emfields *emf);        /* :210-218 */
+void getemf_mhd_test_particle(double x, double y, double z, double t, struct emfields *emf); /* :107-120 */
+void getemf_pic_test_particle(double x, double y, double z, double t, struct emfields *emf); /* :153-166 */
+void get_bfield_mhd_test_particle(double x, double y, double z, double t, struct emfields *emf); /* :131-142 */
+void get_bfield_pic_test_particle(double x, double y, double z, double t, struct emfields *emf); /* :177-188 */
+
+/* --- interpolation (include/interpolation.h:3-10, src/interpolation.c) --- */
+void set_variabls_interpolation(grids *sgrid, domain *sdomain, int mt);                /* :16-21 */
+void grid_indices(double x, double y, double z, double t, int *ix1, int *iy1,
+        int *iz1, int *it1, int *ix2, int *iy2, int *iz2, int *it2,
+        double *dx, double *dy, double *dz, double *dt);                               /* :36-105 */
+void get_trilinar_parameters(double x, double y, double z, double t,
+        long int *corners, double *weights, double *dt);                               /* :141-181 */
+
+/* --- force-free field (include/force_free.h, src/force_free.c) --- */
+void getb_ff(double x, double y, double z, double t, struct bfields *bmf);             /* :138-150 */
+void gete_ff(double x, double y, double z, double t, struct bfields *bmf, struct efields *elf); /* :78-86 */
+void getemf_ff(double x, double y, double z, double t, struct emfields *emf);          /* :54-66 */
+void get_param_ff(int mpi_rank, char *config_file_name);                               /* :99-125 */
+void set_variables_ff(grids *sgrid, domain *sdomain);                                  /* :38-42 */
+
+/* --- wire-loop current systems (include/wlcs.h, src/wlcs.c) --- */
+void read_wlcs(int mpi_rank, char *config_file_name);                                  /* :53-222 */
+void getemf_wlcs(double x, double y, double z, double t, struct emfields *emf_tot);    /* :814-865 */
+void free_config(void);                                                                /* :227-229 */
+void adjust_dt_normI(double *dt);                                                      /* :266-269 */
+
+/* --- gridded fields (include/{magnetic,electric,velocity}_field.h) --- */
+void set_variables_bfield(grids *sgrid, domain *sdomain, double B0_field, int mt, int dtype); /* magnetic_field.c:55-63 */
+void initialize_bfield(void);                                                          /* magnetic_field.c:102-116 */
+void free_bfield(void);                                                                /* magnetic_field.c:144-158 */
+void get_double_bfield_at_point(double x, double y, double z, double t,
+        double *bx, double *by, double *bz);                                           /* magnetic_field.c:555-584 */
+void get_float_bfield_at_point(double x, double y, double z, double t,
+        float *bx, float *by, float *bz);                                              /* magnetic_field.c:593-622 */
+void set_variables_efield(grids *sgrid, domain *sdomain, double E0_field, int mt, int dtype); /* electric_field.c:55-63 */
+void initialize_efield(void);
+void free_efield(void);
+void get_double_efield_at_point(double x, double y, double z, double t,
+        double *ex, double *ey, double *ez);                                           /* electric_field.c:370-399 */
+void get_float_efield_at_point(double x, double y, double z, double t,
+        float *ex, float *ey, float *ez);                                              /* electric_field.c:408-437 */
+void set_variables_velocity(grids *sgrid, domain *sdomain, double v0_field, int mt, int dtype); /* velocity_field.c:55-66 */
+void initialize_vfield(void);
+void free_vfield(void);
+void get_double_velocity_at_point(double x, double y, double z, double t,
+        double *vx, double *vy, double *vz);                                           /* velocity_field.c:555-584 */
+void get_float_velocity_at_point(double x, double y, double z, double t,
+        float *vx, float *vy, float *vz);                                              /* velocity_field.c:593-622 */
+
+/* Reference globals kept under their reference names (src/tracking.c:35-40,
+ * src/emfields.c:16, src/force_free.c:31-33, src/wlcs.c:27-29,
+ * src/magnetic_field.c:31-39, src/electric_field.c:31-39,
+ * src/velocity_field.c:31-39).  The host grid arrays stay owned by the caller
+ * side exactly as in the reference; the library mirrors them on the device. */
+extern grids simul_grid;
+extern domain simul_domain;
+extern int system_type, multi_tframe, bc_flag, data_type;
+extern double charge_mass;
+extern param_ff param;
+extern wlcs *config;
+extern int nwlcs, iBessel;
+extern double normI;
+extern bfields_float *maga_float, *magb_float, *magc_float;
+extern bfields_double *maga_double, *magb_double, *magc_double;
+extern efields_float *efa_float, *efb_float, *efc_float;
+extern efields_double *efa_double, *efb_double, *efc_double;
+extern vfields_float *va_float, *vb_float, *vc_float;
+extern vfields_double *va_double, *vb_double, *vc_double;
+/* Spectrum globals of src/diagnostics.c:32 (set by get_spectrum_info). */
+extern double emin, emax, logemin, logemax, logde;
+
+/* ======================================================================
+ * Part 2: library API
+ * ==================================================================== */
+
+enum {
+    TP_PREC_FP64 = 0,       /* reference arithmetic (no FMA contraction): parity path */
+    TP_PREC_FP64_FAST = 1,  /* FP64 with FMA contraction */
+    TP_PREC_MIXED = 2,      /* FP32 push and field, 64-bit fixed-point positions */
+    TP_PREC_SURROGATE = 3   /* as MIXED with the learned field model (mode-sum field) */
+};
+
+int tp_init(int device);              /* select the GPU; implicit on first use */
+int tp_last_status(void);             /* 0 = ok; sticky until tp_clear_status() */
+const char *tp_last_error(void);
+void tp_clear_status(void);
+int tp_device_status(void);           /* status bits raised by kernels (bounds, limits) */
+
+/* Reference compile-time choices made run-time switches. */
+void tp_set_abc(double A, double B, double C);   /* include/force_free.h:21-26 */
+void tp_set_interp_corrected(int on);            /* x/z weight swap of src/interpolation.c:173-180 */
+void tp_set_ellint_corrected(int on);            /* m >= 0.9 branch of src/wlcs.c:741-804 */
+/* Turbulent plane-wave mode sum (system type TP_SYS_MODESUM), B = B0 z + sum. */
+int tp_set_modes(int nmodes, const tp_mode *modes, double B0);
+/* Spectrum binning (src/diagnostics.c:588-640 without the file): sets
+ * emin, emax, logemin, logemax, logde. */
+void tp_set_spectrum(int nbins, double e_min, double e_max);
+/* Mark the host grid arrays changed after their last upload. */
+void tp_mark_fields_dirty(void);
+
+/* Batch utilities, all on the GPU.  xyzt: n*4 doubles; particles: AoS records. */
+int tp_get_emf_batch(int n, const double *xyzt, double *emf6);
+int tp_wirz_steps(int n, particles *ptl, double dt, int nsteps, int *iescape);
+int tp_energy_bins(int n, const particles *ptl, int nbins, int *bins);
+int tp_calc_diff_coeff_batch(int n, const particles *ptl_init, const particles *ptl,
+                             double dt, double *out8);
+int tp_trilinear_batch(int n, const double *xyzt, long *corners8, double *weights8);
+int tp_energy_thresholds(int nbins, double *thr);  /* nbins-1 exact bin edges */
+
+/* Device-resident tracking sessions. */
+typedef struct tp_session tp_session;
+typedef struct tp_run_info {
+    int estep, einterval, nsdc, nt_out, nbins;
+    int grid, blocks_per_sm;
+    double kernel_ms;          /* device time of the tracking kernel(s), CUDA events */
+    double pushes;             /* particle pushes performed */
+} tp_run_info;
+tp_session *tp_session_create(int nptl);
+void tp_session_destroy(tp_session *s);
+int tp_session_load(tp_session *s, const particles *ptl_init, const particles *ptl);
+int tp_session_track(tp_session *s, int precision, double dt, int nt_out, int nbins,
+                     tp_run_info *info);
+int tp_session_fetch(tp_session *s, particles *ptl, int *nsteps_ptl,
+                     double *espect, double *espect_escape, double *dsum, int *remain);
+
+/* One call, host buffers in and out (reuses a cached session). */
+int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,
+                  const particles *ptl_init, particles *ptl, int *nsteps_ptl,
+                  double *espect, double *espect_escape, double *dsum, int *remain,
+                  tp_run_info *info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TP_GPU_H */

@@ -106,6 +106,7 @@ def oracle():
         _oracle.or_estep.restype = C.c_int
         _oracle.or_track_fixed.restype = C.c_int
         _oracle.or_energy_bin.restype = C.c_int
+        _oracle.or_energy_bin_e.restype = C.c_int
         _oracle.or_bs_integrate.restype = C.c_int
     return _oracle
 

@@ -570,7 +570,11 @@ void or_particle_bc(const or_field *f, particles *p, int *iescape)
 int or_energy_bin(const or_spectrum *s, double ux, double uy, double uz)
 {
     double gama = sqrt(1.0 + ux * ux + uy * uy + uz * uz);
-    double ene = gama - 1.0;
+    return or_energy_bin_e(s, gama - 1.0);
+}
+
+int or_energy_bin_e(const or_spectrum *s, double ene)
+{
     double v = floor((log10(ene) - s->logemin) / s->logde);
     int ibin;
     if (!(v == v) || v < -2147483648.0 || v > 2147483647.0) ibin = (int)0x80000000;

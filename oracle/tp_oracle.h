@@ -57,6 +57,7 @@ void or_ellint(double k, int corrected, double *elle, double *ellk);
 void or_trilinear(const or_field *f, double x, double y, double z, double t,
                   long corners[8], double weights[8], double *dt);
 int or_energy_bin(const or_spectrum *s, double ux, double uy, double uz);
+int or_energy_bin_e(const or_spectrum *s, double ene);  /* bin of an energy gamma - 1 */
 void or_calc_diff_coeff(const or_field *f, const particles *p0, const particles *p,
                         double dt, double out8[8]);
 void or_mode_sum(const or_field *f, double x, double y, double z, emfields *emf);

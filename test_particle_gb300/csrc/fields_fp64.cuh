@@ -1,0 +1,425 @@
+// fields_fp64.cuh -- FP64 field evaluation on the device, reference arithmetic.
+//
+// Each function follows the reference function named in its comment with the
+// same operation order; the translation unit is compiled with -fmad=false so
+// no multiply-add is fused, and sqrt / division are IEEE correctly rounded, so
+// results differ from the reference only where CUDA's sin/cos/acos/log differ
+// from glibc's by an ulp.
+#pragma once
+#include "tp_common.cuh"
+
+#define TP_ELL_QUAL __constant__ static const
+#include "ellint_coeffs.h"
+#undef TP_ELL_QUAL
+
+namespace tp {
+
+#ifndef TP_PI
+#define TP_PI 3.14159265358979323846
+#endif
+
+// get_trilinar_parameters + grid_indices, src/interpolation.c:36-181
+struct Tri64 {
+    long c[8];
+    double w[8];
+    double dt;
+};
+
+__device__ __forceinline__ long idx3(int nx, int ny, int ix, int iy, int iz)
+{
+    long index = ix;          // index_transfer, src/interpolation.c:119-128
+    int shift = nx;
+    index += shift * iy;
+    shift *= ny;
+    index += shift * iz;
+    return index;
+}
+
+__device__ __forceinline__ void trilinear64(const DevField& f, double x, double y, double z,
+                                            double t, Tri64& r)
+{
+    int nx = f.nx, ny = f.ny, nz = f.nz;
+    int ix1 = (int)floor((x - f.xmin) / f.gdx);
+    int iy1 = (int)floor((y - f.ymin) / f.gdy);
+    int iz1 = (int)floor((z - f.zmin) / f.gdz);
+    int ix2 = ix1 + 1, iy2 = iy1 + 1, iz2 = iz1 + 1;
+    double dx = (x - f.xmin) / f.gdx - ix1;
+    double dy = (y - f.ymin) / f.gdy - iy1;
+    double dz = (z - f.zmin) / f.gdz - iz1;
+    if (x > f.xmax) { ix1 = nx - 1; ix2 = 0; dx = x / f.gdx - (nx - 1); }
+    if (y > f.ymax) { iy1 = ny - 1; iy2 = 0; dy = y / f.gdy - (ny - 1); }
+    if (z > f.zmax) { iz1 = nz - 1; iz2 = 0; dz = z / f.gdz - (nz - 1); }
+    if (x < f.xmin) { ix1 = nx - 1; ix2 = 0; dx = x / f.gdx + 1.0; }
+    if (y < f.ymin) { iy1 = ny - 1; iy2 = 0; dy = y / f.gdy + 1.0; }
+    if (z < f.zmin) { iz1 = nz - 1; iz2 = 0; dz = z / f.gdz + 1.0; }
+    if (f.multi_tframe == 0) {
+        r.dt = 0.0;
+    } else {
+        int it1 = (int)floor(t / f.gdt);
+        r.dt = t / f.gdt - it1;
+    }
+    r.c[0] = idx3(nx, ny, ix1, iy1, iz1);
+    r.c[1] = idx3(nx, ny, ix1, iy1, iz2);
+    r.c[2] = idx3(nx, ny, ix1, iy2, iz1);
+    r.c[3] = idx3(nx, ny, ix2, iy1, iz1);
+    r.c[4] = idx3(nx, ny, ix2, iy2, iz1);
+    r.c[5] = idx3(nx, ny, ix2, iy1, iz2);
+    r.c[6] = idx3(nx, ny, ix1, iy2, iz2);
+    r.c[7] = idx3(nx, ny, ix2, iy2, iz2);
+    double ax = 1.0 - dx, ay = 1.0 - dy, az = 1.0 - dz;
+    if (!f.interp_corrected) {
+        // the reference's weights (src/interpolation.c:173-180): corners
+        // 1, 3, 4, 6 carry the weight of their x<->z mirror
+        r.w[0] = ax * ay * az;
+        r.w[1] = dx * ay * az;
+        r.w[2] = ax * dy * az;
+        r.w[3] = ax * ay * dz;
+        r.w[4] = ax * dy * dz;
+        r.w[5] = dx * ay * dz;
+        r.w[6] = dx * dy * az;
+        r.w[7] = dx * dy * dz;
+    } else {
+        r.w[0] = ax * ay * az;
+        r.w[1] = ax * ay * dz;
+        r.w[2] = ax * dy * az;
+        r.w[3] = dx * ay * az;
+        r.w[4] = dx * dy * az;
+        r.w[5] = dx * ay * dz;
+        r.w[6] = ax * dy * dz;
+        r.w[7] = dx * dy * dz;
+    }
+}
+
+__device__ __forceinline__ bool corner_ok(const DevField& f, long c, int* status)
+{
+    long ncell = (long)f.nx * f.ny * f.nz;
+    if (c < 0 || c >= ncell) {
+        if (status) atomicOr(status, ST_BAD_INDEX);
+        return false;
+    }
+    return true;
+}
+
+// get_double_velocity_at_point, src/velocity_field.c:555-584
+__device__ __forceinline__ void interp_d3(const DevField& f, const Tri64& r, const double* c,
+                                          const double* a, const double* b, double out[3],
+                                          int* status)
+{
+    if (f.multi_tframe == 0) {
+        double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            if (!corner_ok(f, r.c[i], status)) continue;
+            const double* p = c + 3 * r.c[i];
+            v0 += p[0] * r.w[i];
+            v1 += p[1] * r.w[i];
+            v2 += p[2] * r.w[i];
+        }
+        out[0] = v0; out[1] = v1; out[2] = v2;
+    } else {
+        double p[3] = {0.0, 0.0, 0.0}, q[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            if (!corner_ok(f, r.c[i], status)) continue;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                p[k] += a[3 * r.c[i] + k] * r.w[i];
+                q[k] += b[3 * r.c[i] + k] * r.w[i];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) out[k] = r.dt * p[k] + (1.0 - r.dt) * q[k];
+    }
+}
+
+// get_float_{b,e}field_at_point / get_float_velocity_at_point,
+// src/magnetic_field.c:593-622: float results accumulated through double
+__device__ __forceinline__ void interp_f3(const DevField& f, const Tri64& r, const float* c,
+                                          const float* a, const float* b, float out[3],
+                                          int* status)
+{
+    if (f.multi_tframe == 0) {
+        float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            if (!corner_ok(f, r.c[i], status)) continue;
+            const float* p = c + 3 * r.c[i];
+            v0 = (float)((double)v0 + (double)__ldg(p + 0) * r.w[i]);
+            v1 = (float)((double)v1 + (double)__ldg(p + 1) * r.w[i]);
+            v2 = (float)((double)v2 + (double)__ldg(p + 2) * r.w[i]);
+        }
+        out[0] = v0; out[1] = v1; out[2] = v2;
+    } else {
+        double p[3] = {0.0, 0.0, 0.0}, q[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            if (!corner_ok(f, r.c[i], status)) continue;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                p[k] += (double)__ldg(a + 3 * r.c[i] + k) * r.w[i];
+                q[k] += (double)__ldg(b + 3 * r.c[i] + k) * r.w[i];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) out[k] = (float)(r.dt * p[k] + (1.0 - r.dt) * q[k]);
+    }
+}
+
+// ---------------------------------------------------------------- WLCS
+// transform / reverse_tran, src/wlcs.c:871-903
+__device__ __forceinline__ void wl_transform(double& ax, double& ay, double& az, double c1,
+                                             double s1, double c2, double s2)
+{
+    double ax1 = c2 * ax + s2 * ay;
+    double ay1 = -s2 * ax + c2 * ay;
+    double az1 = az;
+    ax = c1 * ax1 - s1 * az1;
+    ay = ay1;
+    az = s1 * ax1 + c1 * az1;
+}
+
+__device__ __forceinline__ void wl_reverse(double& ax, double& ay, double& az, double c1,
+                                           double s1, double c2, double s2)
+{
+    double ax1 = c1 * ax + s1 * az;
+    double ay1 = ay;
+    double az1 = -s1 * ax + c1 * az;
+    ax = c2 * ax1 - s2 * ay1;
+    ay = s2 * ax1 + c2 * ay1;
+    az = az1;
+}
+
+// ellint, src/wlcs.c:460-809 (Fukushima 2009), coefficient tables recomputed
+// from the mathematics (gen_ellint_coeffs.py)
+__device__ __forceinline__ void ellint64(double k, int corrected, double& elle, double& ellf)
+{
+    double m = k * k;
+    int i;
+    elle = 0.0;
+    ellf = 0.0;
+    if (m < 0.8) i = (int)(m / 0.1);
+    else if (m >= 0.8 && m < 0.85) i = 8;
+    else if (m >= 0.85 && m < 0.9) i = 9;
+    else i = 10;
+    if (i >= 0 && i <= 9) {
+        double m1 = m - tp_ell_m0[i], powj = 1.0;
+        int nk = tp_ell_nk[i], ne = tp_ell_ne[i];
+        for (int j = 0; j < nk; j++) {
+            double kc = tp_ell_k[i][j];
+            if (!corrected && i == 9 && j == 19) kc = TP_ELL_K9_19_REF;
+            ellf += kc * powj;
+            if (j < ne) elle += tp_ell_e[i][j] * powj;
+            powj *= m1;
+        }
+        return;
+    }
+    double ellf1 = 0.0, q1 = 0.0, hm = 0.0, powj = 1.0;
+    double m1 = corrected ? (0.95 - m) : (m - 0.95);
+    for (int j = 0; j <= 10; j++) {
+        ellf1 += tp_ell_k[0][j] * powj;
+        powj *= m1;
+    }
+    m1 = 1.0 - m;
+    powj = m1;
+    for (int j = 1; j <= 14; j++) {
+        q1 += tp_ell_q[j] * powj;
+        powj *= m1;
+    }
+    powj = 1.0;
+    m1 = 0.95 - m;
+    for (int j = 0; j <= 10; j++) {
+        hm += tp_ell_h[j] * powj;
+        powj *= m1;
+    }
+    ellf = -log(q1) * (ellf1 / TP_PI);
+    elle = 1.0 / ellf1 * (TP_PI / 2.0 + ellf * hm);
+}
+
+// getWireB, src/wlcs.c:361-401
+__device__ __forceinline__ void wl_wire_static(const wlcs& c, double x, double y, double z,
+                                               double B[3])
+{
+    double xp = x - c.x_wr, yp = y - c.y_wr, zp = z - c.z_wr;
+    wl_transform(xp, yp, zp, c.costheta_wr, c.sintheta_wr, c.cosphi_wr, c.sinphi_wr);
+    double rho = sqrt(xp * xp + yp * yp);
+    if (rho < 0.1) rho = 0.1;
+    double cos_phi0 = xp / rho, phi0;
+    if (yp >= 0.0) phi0 = acos(cos_phi0);
+    else phi0 = 2.0 * TP_PI - acos(cos_phi0);
+    double bphi = 1.0 / 5.0 * (c.cur_wr * TP_I0) / (rho * TP_L0);
+    B[0] = bphi * cos(phi0 + TP_PI / 2.0);
+    B[1] = bphi * sin(phi0 + TP_PI / 2.0);
+    B[2] = 0.0;
+    wl_reverse(B[0], B[1], B[2], c.costheta_wr, c.sintheta_wr, c.cosphi_wr, c.sinphi_wr);
+}
+
+// getWire_Bessel, src/wlcs.c:281-355 (single-precision Bessel functions)
+__device__ __forceinline__ void wl_wire_bessel(const wlcs& c, double x, double y, double z,
+                                               double t, double B[3], double E[3])
+{
+    double xp = x - c.x_wr, yp = y - c.y_wr, zp = z - c.z_wr;
+    double t1 = c.t0 + t, curI = c.cur_wr, omega = c.omega, phi1;
+    wl_transform(xp, yp, zp, c.costheta_wr, c.sintheta_wr, c.cosphi_wr, c.sinphi_wr);
+    double rho = sqrt(xp * xp + yp * yp);
+    double x0 = omega * rho * TP_L0 / TP_C0;
+    double bj0 = j0f((float)x0), bj1 = j1f((float)x0);
+    double by0 = y0f((float)x0), by1 = y1f((float)x0);
+    double const0 = (curI * TP_I0) / (5.0 * rho * TP_L0) * TP_PI / 2.0;
+    double wireB = const0 * x0 * (-by1 * cos(omega * t1) + bj1 * sin(omega * t1));
+    if (rho == 0.0) phi1 = TP_PI / 2.0;
+    else if (yp >= 0.0) phi1 = acos(xp / rho) + TP_PI / 2.0;
+    else phi1 = 2.0 * TP_PI - acos(xp / rho) + TP_PI / 2.0;
+    B[0] = wireB * cos(phi1);
+    B[1] = wireB * sin(phi1);
+    B[2] = 0.0;
+    wl_reverse(B[0], B[1], B[2], c.costheta_wr, c.sintheta_wr, c.cosphi_wr, c.sinphi_wr);
+    double wireE = -const0 * x0 * (by0 * sin(omega * t1) + bj0 * cos(omega * t1));
+    E[0] = 0.0; E[1] = 0.0; E[2] = wireE;
+    wl_reverse(E[0], E[1], E[2], c.costheta_wr, c.sintheta_wr, c.cosphi_wr, c.sinphi_wr);
+}
+
+// getLoopB, src/wlcs.c:406-449 (NaN Bx, By on the loop axis, as there)
+__device__ __forceinline__ void wl_loop(const wlcs& c, int ell_corr, double x, double y,
+                                        double z, double B[3])
+{
+    double xp = (x - c.x_lp) * TP_L0, yp = (y - c.y_lp) * TP_L0, zp = (z - c.z_lp) * TP_L0;
+    double al = c.r_lp * TP_L0, curI = c.cur_lp * TP_I0;
+    wl_transform(xp, yp, zp, c.cosbeta_lp, c.sinbeta_lp, c.cosalpha_lp, c.sinalpha_lp);
+    double Irho = 0.2 * curI;
+    double rho_xy = sqrt(xp * xp + yp * yp);
+    double al2 = al * al;
+    double r2 = rho_xy * rho_xy + zp * zp;
+    double irho1 = 1 / sqrt((al + rho_xy) * (al + rho_xy) + zp * zp);
+    double irho2 = 1 / ((al - rho_xy) * (al - rho_xy) + zp * zp);
+    double k = sqrt(4.0 * al * rho_xy) * irho1, elle, ellk;
+    ellint64(k, ell_corr, elle, ellk);
+    double Brho = Irho * zp * irho1 * (-ellk + (al2 + r2) * elle * irho2) / rho_xy;
+    if (rho_xy == 0.0) Brho = 0.0;
+    double Bz = Irho * irho1 * (ellk - (r2 - al2) * elle * irho2);
+    if (ell_corr && rho_xy == 0.0) {
+        B[0] = 0.0; B[1] = 0.0;
+    } else {
+        Brho /= rho_xy;
+        B[0] = Brho * xp;
+        B[1] = Brho * yp;
+    }
+    B[2] = Bz;
+    wl_reverse(B[0], B[1], B[2], c.cosbeta_lp, c.sinbeta_lp, c.cosalpha_lp, c.sinalpha_lp);
+}
+
+// ---------------------------------------------------------------- mode sum
+// Exact phase in 64-bit fixed point: u = (x - min)/L per axis, U = frac(u)*2^64.
+__device__ __forceinline__ uint64_t fixed_frac64(double u)
+{
+    double fr = u - floor(u);
+    return __double2ull_rz(fr * 18446744073709551616.0);
+}
+
+// get_emf, src/emfields.c:32-60, specialised per system type (0..5).
+template <int SYS>
+__device__ __forceinline__ void emf64(const DevField& f, double x, double y, double z, double t,
+                                      double e[6], int* status)
+{
+    e[0] = 0.0; e[1] = 0.0; e[2] = 0.0; e[3] = 0.0; e[4] = 0.0; e[5] = 0.0;
+    if (SYS == TP_SYS_TEST) {
+        e[2] = 1.0E0;  // getemf_test, src/emfields.c:210-218
+    } else if (SYS == TP_SYS_FORCEFREE) {
+        // getb_ff / gete_ff, src/force_free.c:78-86,138-150
+        double l = f.lambda0;
+        double bx = f.ffA * sin(l * z) + f.ffC * cos(l * y);
+        double by = f.ffB * sin(l * x) + f.ffA * cos(l * z);
+        double bz = f.ffC * sin(l * y) + f.ffB * cos(l * x);
+        bx *= f.B0;
+        by *= f.B0;
+        bz *= f.B0;
+        e[0] = bx; e[1] = by; e[2] = bz;
+        if (f.vc_d || f.va_d) {
+            Tri64 r;
+            trilinear64(f, x, y, z, t, r);
+            double v[3];
+            interp_d3(f, r, f.vc_d, f.va_d, f.vb_d, v, status);
+            e[3] = by * v[2] - bz * v[1];
+            e[4] = bz * v[0] - bx * v[2];
+            e[5] = bx * v[1] - by * v[0];
+        }
+    } else if (SYS == TP_SYS_WLCS) {
+        // getemf_wlcs, src/wlcs.c:814-865
+        double Bx = 0.0, By = 0.0, Bz = 0.0, Ex = 0.0, Ey = 0.0, Ez = 0.0;
+        for (int i = 0; i < f.nwlcs; i++) {
+            double B[3], E[3];
+            wlcs c = f.cfg[i];
+            if (f.iBessel == 0) {
+                wl_wire_static(c, x, y, z, B);
+                Bx += B[0]; By += B[1]; Bz += B[2];
+            } else {
+                wl_wire_bessel(c, x, y, z, t, B, E);
+                Bx += B[0]; Ex += E[0];
+                By += B[1]; Ey += E[1];
+                Bz += B[2]; Ez += E[2];
+            }
+            wl_loop(c, f.ellint_corrected, x, y, z, B);
+            Bx += B[0]; By += B[1]; Bz += B[2];
+        }
+        e[0] = Bx; e[1] = By; e[2] = Bz + 0.0;
+        e[3] = Ex; e[4] = Ey; e[5] = Ez;
+    } else if (SYS == TP_SYS_MHD) {
+        // getemf_mhd_test_particle, src/emfields.c:107-120
+        Tri64 r;
+        trilinear64(f, x, y, z, t, r);
+        float v[3], b[3];
+        interp_f3(f, r, f.vc_f, f.va_f, f.vb_f, v, status);
+        interp_f3(f, r, f.bc_f, f.ba_f, f.bb_f, b, status);
+        e[0] = b[0]; e[1] = b[1]; e[2] = b[2];
+        e[3] = e[1] * v[2] - e[2] * v[1];
+        e[4] = e[2] * v[0] - e[0] * v[2];
+        e[5] = e[0] * v[1] - e[1] * v[0];
+    } else if (SYS == TP_SYS_PIC) {
+        // getemf_pic_test_particle, src/emfields.c:153-166; the reference
+        // computes the same corners and weights twice, once is enough
+        Tri64 r;
+        trilinear64(f, x, y, z, t, r);
+        float ev[3], b[3];
+        interp_f3(f, r, f.ec_f, f.ea_f, f.eb_f, ev, status);
+        interp_f3(f, r, f.bc_f, f.ba_f, f.bb_f, b, status);
+        e[3] = ev[0]; e[4] = ev[1]; e[5] = ev[2];
+        e[0] = b[0]; e[1] = b[1]; e[2] = b[2];
+    } else if (SYS == TP_SYS_MODESUM) {
+        uint64_t ux = fixed_frac64((x - f.xmin) / (f.xmax - f.xmin));
+        uint64_t uy = fixed_frac64((y - f.ymin) / (f.ymax - f.ymin));
+        uint64_t uz = fixed_frac64((z - f.zmin) / (f.zmax - f.zmin));
+        double b0 = 0.0, b1 = 0.0, b2 = 0.0, e0 = 0.0, e1 = 0.0, e2 = 0.0;
+        for (int m = 0; m < f.nmodes; m++) {
+            const tp_mode& md = f.modes[m];
+            // md.pad holds the 32-bit fixed-point phase offset (host-filled)
+            uint64_t ph = (uint64_t)(int64_t)md.n[0] * ux + (uint64_t)(int64_t)md.n[1] * uy +
+                          (uint64_t)(int64_t)md.n[2] * uz +
+                          ((uint64_t)(uint32_t)md.pad << 32);
+            double th = (double)(int64_t)ph * (2.0 * TP_PI / 18446744073709551616.0);
+            double c = cos(th);
+            b0 += md.amp_b[0] * c; b1 += md.amp_b[1] * c; b2 += md.amp_b[2] * c;
+            e0 += md.amp_e[0] * c; e1 += md.amp_e[1] * c; e2 += md.amp_e[2] * c;
+        }
+        e[0] = b0; e[1] = b1; e[2] = f.B0 + b2;
+        e[3] = e0; e[4] = e1; e[5] = e2;
+    }
+}
+
+// Same, dispatched at run time (batch utilities; the tracking kernels are
+// instantiated per system type).
+__device__ __forceinline__ void emf64_dispatch(const DevField& f, double x, double y, double z,
+                                               double t, double e[6], int* status)
+{
+    switch (f.system_type) {
+    case TP_SYS_TEST: emf64<TP_SYS_TEST>(f, x, y, z, t, e, status); break;
+    case TP_SYS_WLCS: emf64<TP_SYS_WLCS>(f, x, y, z, t, e, status); break;
+    case TP_SYS_FORCEFREE: emf64<TP_SYS_FORCEFREE>(f, x, y, z, t, e, status); break;
+    case TP_SYS_MHD: emf64<TP_SYS_MHD>(f, x, y, z, t, e, status); break;
+    case TP_SYS_PIC: emf64<TP_SYS_PIC>(f, x, y, z, t, e, status); break;
+    case TP_SYS_MODESUM: emf64<TP_SYS_MODESUM>(f, x, y, z, t, e, status); break;
+    default:
+        e[0] = e[1] = e[2] = e[3] = e[4] = e[5] = 0.0;
+        break;
+    }
+}
+
+}  // namespace tp

@@ -1,0 +1,308 @@
+// session.cu -- device-resident tracking sessions: particle state in HBM as
+// SoA, one persistent tracking launch per run, diagnostics reduced on the GPU.
+#include <cmath>
+#include <cstring>
+
+#include "../../include/tp_gpu.h"
+#include "tp_internal.h"
+#include "tp_kernels.h"
+#include "tp_session.h"
+
+namespace tp {
+
+__global__ void fill_int_kernel(int* p, int n, int v)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+static void fill_int(int* p, int n, int v, cudaStream_t s)
+{
+    if (n > 0) fill_int_kernel<<<(n + 255) / 256, 256, 0, s>>>(p, n, v);
+}
+
+Session::~Session()
+{
+    for (Scratch* sc : {&soa, &soa0, &aos, &nsteps, &spec, &rem, &dpart, &dsum, &traj, &trajacc,
+                        &trajpts})
+        sc->release();
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+}
+
+bool Session::reserve(int n)
+{
+    if (!ensure_init()) return false;
+    if (!ev0) {
+        cudaEventCreate(&ev0);
+        cudaEventCreate(&ev1);
+    }
+    if (n <= cap) return true;
+    size_t rec = sizeof(double) * 11 * (size_t)n;
+    if (!soa.get(rec) || !soa0.get(rec) || !aos.get(rec) || !nsteps.get(sizeof(int) * (size_t)n))
+        return false;
+    cap = n;
+    return true;
+}
+
+bool Session::load(const particles* ptl_init, const particles* ptl, int n_)
+{
+    if (!reserve(n_)) return false;
+    n = n_;
+    cudaStream_t s = g.stream;
+    double* a = (double*)aos.ptr;
+    if (n > 0) {
+        if (!cuda_ok(cudaMemcpyAsync(a, ptl_init, sizeof(particles) * n, cudaMemcpyHostToDevice, s),
+                     "load init")) return false;
+        aos_to_soa(a, n, (double*)soa0.ptr, cap, s);
+        if (!cuda_ok(cudaMemcpyAsync(a, ptl, sizeof(particles) * n, cudaMemcpyHostToDevice, s),
+                     "load ptl")) return false;
+        aos_to_soa(a, n, (double*)soa.ptr, cap, s);
+    }
+    loaded = true;
+    return cuda_ok(cudaGetLastError(), "load");
+}
+
+bool Session::run(const RunSpec& rs, tp_run_info* info)
+{
+    if (!loaded) {
+        set_error(1, "session: particles not loaded");
+        return false;
+    }
+    if (rs.estep < rs.sstep || rs.einterval < 1 || rs.nt_out < 1) {
+        set_error(6, "bad step range: sstep %d estep %d einterval %d nt_out %d", rs.sstep, rs.estep,
+                  rs.einterval, rs.nt_out);
+        return false;
+    }
+    DevField f;
+    if (!build_field(system_type, f)) return false;
+    if (!ensure_thresholds(rs.nbins)) return false;
+    cudaStream_t s = g.stream;
+    nt_out = rs.nt_out;
+    nbins = rs.nbins;
+    nsdc = rs.estep / kDiffInterval + 1;
+    const int ntiles = (n + kBlock - 1) / kBlock;
+    int bps = 0;
+    if (rs.precision == TP_PREC_FP64) bps = fp64::track_max_blocks_per_sm(system_type);
+    else if (rs.precision == TP_PREC_FP64_FAST) bps = fp64fast::track_max_blocks_per_sm(system_type);
+    else {
+        set_error(1, "precision %d not available for system type %d", rs.precision, system_type);
+        return false;
+    }
+    if (bps < 1) bps = 1;
+    int grid = g.num_sms * bps;
+    if (grid > ntiles) grid = ntiles;
+    if (grid < 1) grid = 1;
+    size_t nspec = (size_t)nt_out * nbins;
+    unsigned* d_spec = (unsigned*)spec.get(sizeof(unsigned) * 2 * nspec);
+    int* d_rem = (int*)rem.get(sizeof(int) * nsdc);
+    double* d_dpart = (double*)dpart.get(sizeof(double) * 8 * (size_t)nsdc * grid);
+    double* d_dsum = (double*)dsum.get(sizeof(double) * 8 * (size_t)nsdc);
+    if (!d_spec || !d_rem || !d_dpart || !d_dsum) return false;
+    cudaMemsetAsync(d_spec, 0, sizeof(unsigned) * 2 * nspec, s);
+    cudaMemsetAsync(d_rem, 0, sizeof(int) * nsdc, s);
+    cudaMemsetAsync(d_dpart, 0, sizeof(double) * 8 * (size_t)nsdc * grid, s);
+    if (rs.reset_nsteps) fill_int((int*)nsteps.ptr, n, 1, s);
+
+    TrackBufs b;
+    memset(&b, 0, sizeof(b));
+    double* S = (double*)soa.ptr;
+    double* S0 = (double*)soa0.ptr;
+    long st = cap;
+    b.x = S; b.y = S + st; b.z = S + 2 * st; b.qm = S + 3 * st;
+    b.ux = S + 4 * st; b.uy = S + 5 * st; b.uz = S + 6 * st; b.t = S + 7 * st;
+    b.xs = S + 8 * st; b.ys = S + 9 * st; b.zs = S + 10 * st;
+    b.x0 = S0; b.y0 = S0 + st; b.z0 = S0 + 2 * st;
+    b.ux0 = S0 + 4 * st; b.uy0 = S0 + 5 * st; b.uz0 = S0 + 6 * st; b.t0 = S0 + 7 * st;
+    b.nsteps_ptl = (int*)nsteps.ptr;
+    b.ebin_thr = g.d_thr;
+    b.espect = d_spec;
+    b.espect_esc = d_spec + nspec;
+    b.remain = d_rem;
+    b.dpart = d_dpart;
+    b.status = g.d_status;
+    if (rs.traj_every > 0) {
+        b.ptl_time = (double*)traj.ptr;
+        b.ntraj_accum = (const int*)trajacc.ptr;
+        b.ntraj_points = (int*)trajpts.ptr;
+        b.ntraj_total = traj_total;
+    }
+    TrackParams q;
+    q.n = n;
+    q.estep = rs.estep;
+    q.einterval = rs.einterval;
+    q.nt_out = nt_out;
+    q.nbins = nbins;
+    q.nsdc = nsdc;
+    q.ntp0 = (int)floor(rs.sstep / (double)rs.einterval);
+    q.ntiles = ntiles;
+    q.sstep = rs.sstep;
+    q.traj_every = rs.traj_every;
+    q.dt = rs.dt;
+    cudaEventRecord(ev0, s);
+    cudaError_t e = rs.precision == TP_PREC_FP64 ? fp64::launch_track(f, b, q, grid, s)
+                                                 : fp64fast::launch_track(f, b, q, grid, s);
+    if (!cuda_ok(e, "track launch")) return false;
+    cudaEventRecord(ev1, s);
+    if (!cuda_ok(fp64::launch_reduce_dpart(d_dpart, grid, nsdc, d_dsum, s), "reduce")) return false;
+    if (!cuda_ok(cudaStreamSynchronize(s), "track")) return false;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    last_ms = ms;
+    if (info) {
+        info->estep = rs.estep;
+        info->einterval = rs.einterval;
+        info->nsdc = nsdc;
+        info->nt_out = nt_out;
+        info->nbins = nbins;
+        info->grid = grid;
+        info->blocks_per_sm = bps;
+        info->kernel_ms = ms;
+        info->pushes = (double)n * (rs.estep - rs.sstep + 1);
+    }
+    return true;
+}
+
+bool Session::fetch(particles* ptl, int* nsteps_ptl, double* espect, double* espect_escape,
+                    double* dsum_out, int* remain)
+{
+    cudaStream_t s = g.stream;
+    if (ptl && n > 0) {
+        soa_to_aos((const double*)soa.ptr, n, cap, (double*)aos.ptr, s);
+        cudaMemcpyAsync(ptl, aos.ptr, sizeof(particles) * n, cudaMemcpyDeviceToHost, s);
+    }
+    if (nsteps_ptl && n > 0)
+        cudaMemcpyAsync(nsteps_ptl, nsteps.ptr, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
+    size_t nspec = (size_t)nt_out * nbins;
+    std::vector<unsigned> hs;
+    if ((espect || espect_escape) && nspec) {
+        hs.resize(2 * nspec);
+        cudaMemcpyAsync(hs.data(), spec.ptr, sizeof(unsigned) * 2 * nspec, cudaMemcpyDeviceToHost, s);
+    }
+    if (dsum_out && nsdc)
+        cudaMemcpyAsync(dsum_out, dsum.ptr, sizeof(double) * 8 * nsdc, cudaMemcpyDeviceToHost, s);
+    if (remain && nsdc)
+        cudaMemcpyAsync(remain, rem.ptr, sizeof(int) * nsdc, cudaMemcpyDeviceToHost, s);
+    if (!cuda_ok(cudaStreamSynchronize(s), "fetch")) return false;
+    if (espect)
+        for (size_t k = 0; k < nspec; k++) espect[k] = (double)hs[k];
+    if (espect_escape)
+        for (size_t k = 0; k < nspec; k++) espect_escape[k] = (double)hs[nspec + k];
+    return true;
+}
+
+bool Session::set_traj(const int* ntraj_accum, const particles* ptl_time, int* points)
+{
+    if (n <= 0) return true;
+    traj_total = ntraj_accum[n - 1];
+    if (traj_total < 0) traj_total = 0;
+    if (!traj.get(sizeof(particles) * (size_t)(traj_total > 0 ? traj_total : 1)) ||
+        !trajacc.get(sizeof(int) * (size_t)n) || !trajpts.get(sizeof(int) * (size_t)n))
+        return false;
+    cudaStream_t s = g.stream;
+    if (traj_total > 0 && ptl_time)
+        cudaMemcpyAsync(traj.ptr, ptl_time, sizeof(particles) * traj_total, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(trajacc.ptr, ntraj_accum, sizeof(int) * n, cudaMemcpyHostToDevice, s);
+    if (points) cudaMemcpyAsync(trajpts.ptr, points, sizeof(int) * n, cudaMemcpyHostToDevice, s);
+    else fill_int((int*)trajpts.ptr, n, 1, s);
+    return cuda_ok(cudaGetLastError(), "traj");
+}
+
+bool Session::get_traj(particles* ptl_time, int* points)
+{
+    cudaStream_t s = g.stream;
+    if (ptl_time && traj_total > 0)
+        cudaMemcpyAsync(ptl_time, traj.ptr, sizeof(particles) * traj_total, cudaMemcpyDeviceToHost, s);
+    if (points && n > 0) cudaMemcpyAsync(points, trajpts.ptr, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
+    return cuda_ok(cudaStreamSynchronize(s), "traj fetch");
+}
+
+Session& cached_session()
+{
+    static Session* s = new Session();
+    return *s;
+}
+
+// estep, einterval as particle_tracking_fixed_time_step derives them (src/tracking.c:103-109)
+bool derive_steps(double dt, int nt_out, int& estep, int& einterval)
+{
+    if (!(dt > 0.0) || nt_out < 1) {
+        set_error(6, "bad dt %g or nt_out %d", dt, nt_out);
+        return false;
+    }
+    estep = (int)(simul_domain.tmax / dt);
+    if (estep < 1) {
+        set_error(6, "tmax %g / dt %g gives no steps", simul_domain.tmax, dt);
+        return false;
+    }
+    einterval = estep / nt_out;
+    if (einterval < 1) {
+        set_error(6, "fewer steps (%d) than diagnostic frames (%d)", estep, nt_out);
+        return false;
+    }
+    return true;
+}
+
+}  // namespace tp
+
+using namespace tp;
+
+struct tp_session {
+    Session s;
+};
+
+extern "C" tp_session* tp_session_create(int nptl)
+{
+    tp_session* s = new tp_session();
+    if (!s->s.reserve(nptl)) {
+        delete s;
+        return nullptr;
+    }
+    return s;
+}
+
+extern "C" void tp_session_destroy(tp_session* s) { delete s; }
+
+extern "C" int tp_session_load(tp_session* s, const particles* ptl_init, const particles* ptl)
+{
+    return s && s->s.load(ptl_init, ptl, s->s.cap) ? 0 : -1;
+}
+
+extern "C" int tp_session_track(tp_session* s, int precision, double dt, int nt_out, int nbins,
+                                tp_run_info* info)
+{
+    if (!s) return -1;
+    RunSpec rs;
+    if (!derive_steps(dt, nt_out, rs.estep, rs.einterval)) return -1;
+    rs.precision = precision;
+    rs.dt = dt;
+    rs.nt_out = nt_out;
+    rs.nbins = nbins;
+    return s->s.run(rs, info) ? 0 : -1;
+}
+
+extern "C" int tp_session_fetch(tp_session* s, particles* ptl, int* nsteps_ptl, double* espect,
+                                double* espect_escape, double* dsum, int* remain)
+{
+    return s && s->s.fetch(ptl, nsteps_ptl, espect, espect_escape, dsum, remain) ? 0 : -1;
+}
+
+extern "C" int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,
+                             const particles* ptl_init, particles* ptl, int* nsteps_ptl,
+                             double* espect, double* espect_escape, double* dsum, int* remain,
+                             tp_run_info* info)
+{
+    Session& s = cached_session();
+    RunSpec rs;
+    if (!derive_steps(dt, nt_out, rs.estep, rs.einterval)) return -1;
+    rs.precision = precision;
+    rs.dt = dt;
+    rs.nt_out = nt_out;
+    rs.nbins = nbins;
+    if (!s.load(ptl_init, ptl, nptl)) return -1;
+    if (!s.run(rs, info)) return -1;
+    if (!s.fetch(ptl, nsteps_ptl, espect, espect_escape, dsum, remain)) return -1;
+    if (remain)  // the kernel counts departures; the reference starts from nptl
+        for (int k = 0; k < s.nsdc; k++) remain[k] += nptl;
+    return 0;
+}

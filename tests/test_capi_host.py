@@ -1,0 +1,138 @@
+"""C ABI without a GPU: the library builds, loads and exports every function
+include/tp_gpu.h declares; host-only logic (exact bin edges, init.dat parsers,
+scalar helpers) runs without touching CUDA."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import make_golden as mg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from test_particle_gb300 import build
+    build.build()
+    import test_particle_gb300 as tp
+    return tp.lib()
+
+
+def declared_functions():
+    names = []
+    for fn in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not fn.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", fn)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b([a-z_][a-z0-9_]*)\s*\(", src, flags=re.M):
+            if not src[m.start():].lstrip().startswith(("typedef", "#")):
+                names.append(m.group(1))
+    return sorted(set(names))
+
+
+def test_exports_every_declared_function(lib):
+    names = declared_functions()
+    assert len(names) > 60
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_exports_reference_globals(lib):
+    for name in ("simul_grid", "simul_domain", "system_type", "multi_tframe", "bc_flag",
+                 "charge_mass", "param", "config", "nwlcs", "iBessel", "magc_float",
+                 "efc_float", "vc_double", "emin", "logemin", "logde"):
+        C.c_int.in_dll(lib, name)
+
+
+def test_bin_edges_reproduce_reference_bins(lib):
+    """Bins from the host-derived edges equal the reference's glibc formula."""
+    import test_particle_gb300 as tp
+    eb = np.load(os.path.join(mg.HERE, "ebins.npz"))
+    nb = int(eb["nbins"])
+    tp.set_spectrum(nb, float(eb["emin"]), float(eb["emax"]))
+    thr = tp.energy_thresholds(nb)
+    assert np.all(np.diff(thr) > 0)
+    p = eb["ptl"]
+    e = np.sqrt(1.0 + p["ux"] ** 2 + p["uy"] ** 2 + p["uz"] ** 2) - 1.0
+    bins = np.searchsorted(thr, e, side="right")
+    bins[~np.isfinite(e)] = 0
+    assert np.array_equal(bins, eb["bins"])
+
+
+def test_bin_edges_are_tight(lib):
+    """Each edge is the smallest double of its bin under the reference formula."""
+    import test_particle_gb300 as tp
+    from oracle import pyoracle as po
+    for nb, e0, e1 in ((50, 1e-4, 10.0), (200, 1e-3, 1e2), (162, 1e-5, 1e3)):
+        tp.set_spectrum(nb, e0, e1)
+        thr = tp.energy_thresholds(nb)
+        s = po.spectrum(nb, e0, e1)
+        ob = po.oracle().or_energy_bin_e
+        for b, t in enumerate(thr, start=1):
+            assert ob(C.byref(s), C.c_double(t)) >= b
+            assert ob(C.byref(s), C.c_double(np.nextafter(t, 0))) < b
+
+
+def test_parsers(lib, tmp_path):
+    init = tmp_path / "init.dat"
+    init.write_text(
+        "--------------------------------- System info --------------------------------\n"
+        "0: test, 1: wlcs, 2: forcefree 3: MHD+test particle 4: PIC fields+test particle\n"
+        "Flag for the system to use: 1\n"
+        "Number of WLCSs: 2\n"
+        "Configuration file name: %s\n"
+        "------------------------------ Force-free field ------------------------------\n"
+        "Normalized B(Gauss): 2.5\n"
+        "1/Length scale (lambda): 6.25\n"
+        "------------------------------ Particle tracking -----------------------------\n"
+        "Total tracking time (s): 100.0\n"
+        "0 for fixed step, 1 for adaptive\n"
+        "Tracking method to use: 0\n"
+        "Tracking time step (for electrons): 1E-2\n" % (tmp_path / "wl.dat"))
+    (tmp_path / "wl.dat").write_text(
+        "== header ==\n"
+        "1.0 0.5 0.5 0.5 0.3 0.7 0.0 2.0 1.0 0.4 0.6 0.5 0.1 0.2\n"
+        "0.5 0.1 0.2 0.3 0.0 0.0 1.0 1.0 0.5 0.5 0.5 0.5 0.0 0.0\n"
+        "0\n0.002\n0.25\n")
+    lib.get_tracking_time_interval.restype = C.c_double
+    assert lib.get_tracking_time_interval(0, str(init).encode(), C.c_double(2.0)) == 2e-2
+    lib.get_param_ff(0, str(init).encode())
+    import test_particle_gb300 as tp
+    prm = tp.ParamFF.in_dll(lib, "param")
+    assert (prm.B0, prm.lambda0) == (2.5, 6.25)
+    lib.read_wlcs(0, str(init).encode())
+    assert C.c_int.in_dll(lib, "nwlcs").value == 2
+    cfg = C.cast(C.c_void_p.in_dll(lib, "config").value, C.POINTER(tp.Wlcs))
+    assert cfg[0].cur_wr == 0.25 and cfg[0].cur_lp == 0.5 and cfg[1].omega == 0.002
+    assert abs(cfg[0].costheta_wr - np.cos(0.3)) < 1e-15 and abs(cfg[0].sinbeta_lp - np.sin(0.2)) < 1e-15
+    dt = C.c_double(1.0)
+    lib.adjust_dt_normI(C.byref(dt))
+    assert abs(dt.value - 1.0 / 0.25 / 2.0) < 1e-15
+    lib.free_config()
+
+
+def test_scalar_helpers(lib):
+    assert lib.getgamma(C.c_double(3.0), C.c_double(0.0), C.c_double(4.0)) == np.sqrt(26.0)
+    assert lib.modulus(C.c_double(3.0), C.c_double(4.0), C.c_double(12.0)) == 13.0
+    cx, cy, cz = C.c_double(), C.c_double(), C.c_double()
+    lib.cross_product(C.c_double(1), C.c_double(0), C.c_double(0), C.c_double(0), C.c_double(1),
+                      C.c_double(0), C.byref(cx), C.byref(cy), C.byref(cz))
+    assert (cx.value, cy.value, cz.value) == (0.0, 0.0, 1.0)
+
+
+def test_no_gpu_is_an_error_not_a_fallback(lib):
+    """Without a device the compute entry points fail loudly."""
+    import test_particle_gb300 as tp
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(RuntimeError, match="no CUDA device"):
+        tp.get_emf(np.zeros((1, 4)))

@@ -1,0 +1,158 @@
+"""CUDA path (through the C ABI) against the golden vectors produced by the
+reference's own sources, and against the oracle.
+
+Tolerances: the FP64 parity path uses the reference's operation order without
+FMA contraction, so gridded-field evaluation (no transcendental functions) is
+bit-exact; where the reference calls sin/cos/acos/log, CUDA's libm may differ
+from glibc's by an ulp, hence 1e-12 relative for one step (the single-step bar)
+and looser bounds after many chaotic steps.
+"""
+import json
+
+import numpy as np
+import pytest
+
+import make_golden as mg
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+tp = pytest.importorskip("test_particle_gb300")
+SC = mg.scenarios()
+NAMES = ("test", "ff_vel", "abc111", "mhd", "pic", "pic_mt", "pic_off", "wlcs", "loop")
+EXACT = ("test", "mhd", "pic", "pic_mt", "pic_off")  # no transcendental functions
+
+
+def load(name):
+    return np.load("%s/%s.npz" % (mg.HERE, name))
+
+
+def configure(name, bc_flag=0, **kw):
+    s = dict(SC[name])
+    s.update(kw)
+    tp.configure(system_type=s["system_type"], charge_mass=s["charge_mass"], bc_flag=bc_flag,
+                 dom=s["dom"], grd=s["grd"], mt=s["mt"],
+                 abc=s.get("abc", (1.0, np.sqrt(2 / 3.0), np.sqrt(1 / 3.0))),
+                 B0=s.get("B0", 1.0), lambda0=s.get("lambda0", 1.0), vgrid_d=s.get("vgrid_d"),
+                 vgrid_f=s.get("vgrid_f"), bgrid=s.get("bgrid"), egrid=s.get("egrid"),
+                 bgrid_ab=s.get("bgrid_ab", (None, None)), egrid_ab=s.get("egrid_ab", (None, None)),
+                 wl=s.get("wl"), ibessel=s.get("ibessel", 0))
+
+
+def rel_err(a, b):
+    scale = np.maximum(np.abs(b), 1e-300)
+    return np.nanmax(np.abs(a - b) / np.maximum(scale, np.max(np.abs(b)) * 1e-12))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_get_emf(name):
+    emf = load("emf")
+    configure(name)
+    out = tp.get_emf(emf[name + "_xyzt"])
+    ref = emf[name + "_emf"]
+    if name in EXACT:
+        assert np.array_equal(out, ref, equal_nan=True)
+    else:
+        assert np.array_equal(np.isnan(out), np.isnan(ref))
+        ok = ~np.isnan(ref)
+        np.testing.assert_allclose(out[ok], ref[ok], rtol=1e-13, atol=1e-13 * np.abs(ref[ok]).max())
+    assert tp.device_status() == 0
+
+
+def test_trilinear_exact():
+    tl = load("trilinear")
+    configure("pic_off")
+    c, w = tp.trilinear(tl["xyzt"])
+    assert np.array_equal(c, tl["corners"]) and np.array_equal(w, tl["weights"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_wirz_single_step(name):
+    """One push: within 1e-12 relative of the reference per particle."""
+    wz = load("wirz")
+    configure(name, bc_flag=2 if name in ("wlcs", "loop") else 0)
+    out, _ = tp.wirz_steps(wz[name + "_in"], float(wz[name + "_dt"]), 1)
+    ref = wz[name + "_out1"]
+    for k in ("x", "y", "z", "ux", "uy", "uz", "t"):
+        a, b = out[k], ref[k]
+        if name in ("test",):
+            assert np.array_equal(a, b) or np.max(np.abs(a - b) / np.maximum(np.abs(b), 1)) < 1e-15
+        err = np.max(np.abs(a - b) / np.maximum(np.abs(b), np.abs(ref[k]).max() * 1e-3 + 1e-300))
+        assert err < 1e-12, (k, err)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_wirz_40_steps(name):
+    wz = load("wirz")
+    configure(name, bc_flag=2 if name in ("wlcs", "loop") else 0)
+    out, _ = tp.wirz_steps(wz[name + "_in"], float(wz[name + "_dt"]), 40)
+    ref = wz[name + "_out40"]
+    for k in ("x", "y", "z", "ux", "uy", "uz"):
+        err = np.max(np.abs(out[k] - ref[k]) / (np.abs(ref[k]).max() + 1e-300))
+        assert err < 1e-9, (k, err)
+
+
+def test_energy_bins_exact():
+    """Histogram bins bit-exact for identical energies (edges derived on the host)."""
+    eb = load("ebins")
+    tp.set_spectrum(int(eb["nbins"]), float(eb["emin"]), float(eb["emax"]))
+    bins = tp.energy_bins(eb["ptl"], int(eb["nbins"]))
+    assert np.array_equal(bins, eb["bins"])
+
+
+def test_calc_diff_coeff():
+    dc = load("diffcoeff")
+    configure("ff_vel")
+    out = tp.calc_diff_coeff(dc["p0"], dc["p"], float(dc["dt"]))
+    np.testing.assert_allclose(out, dc["out"], rtol=1e-11, atol=1e-14)
+
+
+@pytest.mark.parametrize("case", range(7))
+def test_track_fixed(case):
+    tr = load("track")
+    key = "case%d_" % case
+    m = json.loads(str(tr[key + "meta"]))
+    s = dict(SC[m["name"]])
+    d = po.Domain.from_buffer_copy(s["dom"])
+    d.tmax = m["tmax"]
+    configure(m["name"], bc_flag=m["bc"], dom=d)
+    tp.set_spectrum(m["nbins"], m["emin"], m["emax"])
+    out = tp.track(tr[key + "ptl0"], m["dt"], m["nt_out"], m["nbins"], precision=tp.PREC_FP64)
+    ref_p = tr[key + "ptl"]
+    exact = m["name"] in EXACT
+    for k in ("x", "y", "z", "ux", "uy", "uz", "t", "xshift", "yshift", "zshift"):
+        if exact:
+            assert np.array_equal(out["ptl"][k], ref_p[k]), k
+        else:
+            err = np.max(np.abs(out["ptl"][k] - ref_p[k]) / (np.abs(ref_p[k]).max() + 1e-300))
+            assert err < 1e-6, (k, err)
+    assert np.array_equal(out["nsteps"], tr[key + "nsteps"])
+    assert np.array_equal(out["remain"], tr[key + "remain"])
+    if exact:
+        assert np.array_equal(out["espect"], tr[key + "espect"])
+        assert np.array_equal(out["espect_escape"], tr[key + "espect_escape"])
+    else:
+        assert out["espect"].sum() == tr[key + "espect"].sum()
+        assert np.abs(out["espect"] - tr[key + "espect"]).sum() <= 2 * m["nt_out"]
+    np.testing.assert_allclose(out["dsum"], tr[key + "dsum"], rtol=1e-9 if exact else 1e-5,
+                               atol=1e-12)
+    assert tp.device_status() == 0
+
+
+def test_track_larger_vs_oracle():
+    """4096 particles x 1000 steps in the ABC field: GPU FP64 vs the oracle."""
+    rng = np.random.default_rng(3)
+    s = dict(SC["abc111"])
+    d = po.Domain.from_buffer_copy(s["dom"])
+    dt = 0.02
+    d.tmax = 1000 * dt + dt / 2
+    configure("abc111", dom=d)
+    tp.set_spectrum(200, 1e-3, 1e2)
+    p0 = mg.particles_for(dict(s, dom=d), rng, 4096)
+    out = tp.track(p0, dt, 10, 200)
+    f = mg.field_from(dict(s, dom=d))
+    ref = po.track_fixed(f, po.spectrum(200, 1e-3, 1e2), p0, dt, 10, nthreads=0)
+    for k in ("x", "y", "z", "ux", "uy", "uz"):
+        assert np.max(np.abs(out["ptl"][k] - ref["ptl"][k])) < 1e-5
+    assert np.abs(out["espect"] - ref["espect"]).sum() <= 40
+    np.testing.assert_allclose(out["dsum"], ref["dsum"], rtol=1e-5, atol=1e-12)
