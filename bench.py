@@ -1,0 +1,320 @@
+"""Benchmark: particle pushes per second on one GB300.
+
+Workload (the configuration the headline metric is quoted on): gridded
+PIC-style fields on a 512^3 periodic grid (6 FP32 components, synthesised on
+the GPU from seeded Kolmogorov modes, B0 = 1 along z, dB/B0 = 0.5,
+E = -v x B from a velocity field of rms 0.1), trilinear interpolation,
+1,048,576 particles per GPU at |v| = 0.7c, 5,000 Wirz steps per run with the
+fused energy-spectrum and diffusion-coefficient diagnostics.  One bench step
+is one such run (5.24e9 pushes).  The field (4.3 GB node-interleaved FP32 plus
+the 3.2 GB reference AoS copy) is far larger than L2, so no L2 flush is needed
+between steps.
+
+value: mixed-precision path (FP32 push and field, 64-bit fixed-point
+positions), particles resident in HBM.  e2e: the same through the C ABI with
+host buffers (particles copied in and results copied out every step).  The
+FP64 parity path is measured on the same workload and reported beside it.
+
+python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-pushes/s on 1 GB300: FP64 vs mixed+surrogate at stated spectrum error"
+UNIT = "pushes/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (reads settings only)."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % self.device)
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=index,clocks.sm,clocks.max.sm,"
+                 "power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+            sm = [float(r[1]) for r in rows]
+            mx = [float(r[2]) for r in rows]
+            reasons = set()
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for r in rows:
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            return {"sm_mhz": float(np.median(sm)) if sm else None,
+                    "sm_max_mhz": max(mx) if mx else None, "samples": len(rows),
+                    "reasons": sorted(reasons)}
+        except Exception as e:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "error": str(e)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def setup_grid(tp, wl, cfg, rank, to_host=False):
+    n = cfg["n"]
+    dom = tp.Domain()
+    dom.xmin, dom.ymin, dom.zmin = cfg["lo"]
+    dom.xmax, dom.ymax, dom.zmax = cfg["hi"]
+    dom.xmin_ptl, dom.ymin_ptl, dom.zmin_ptl = cfg["lo"]
+    dom.xmax_ptl, dom.ymax_ptl, dom.zmax_ptl = cfg["hi"]
+    dom.tmax = cfg["steps"] * cfg["dt"] + 0.5 * cfg["dt"]
+    grd = tp.Grids()
+    grd.nx = grd.ny = grd.nz = n
+    grd.nt = 1
+    grd.dx = grd.dy = grd.dz = cfg["dx"]
+    tp.configure(system_type=tp.SYS_PIC, charge_mass=1.0, bc_flag=0, dom=dom, grd=grd, mt=0)
+    mb = wl.kolmogorov_modes(cfg["nmodes"], cfg["kmin"], cfg["kmax"], cfg["dB"], cfg["seed"])
+    mv = wl.kolmogorov_modes(cfg["nmodes"], cfg["kmin"], cfg["kmax"], cfg["v_rms"], cfg["seed"] + 1000)
+    he, hb = tp.synth_pic_fields(mb, mv, 1.0, to_host=to_host)
+    tp.set_spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
+    p0 = wl.shell_particles(cfg["nptl"], cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"] + 7 * rank)
+    return dom, grd, p0, he, hb
+
+
+def cpu_baseline(cfg, dom, grd, he, hb, target_s=12.0):
+    """The oracle (CPU restatement of the reference's FP64 path) on every host
+    core, on a bounded sample of the same workload."""
+    from oracle import pyoracle as po
+    import test_particle_gb300.workloads as wl
+    cores = os.cpu_count() or 1
+    d = po.Domain.from_buffer_copy(dom)
+    g = po.Grids.from_buffer_copy(grd)
+    f = po.make_field(system_type=4, charge_mass=1.0, bc_flag=0, dom=d, grd=g, egrid=he, bgrid=hb)
+    s = po.spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
+    dt = cfg["dt"]
+
+    def run(nptl, nsteps):
+        d.tmax = nsteps * dt + 0.5 * dt
+        f.dom = d
+        p = wl.shell_particles(nptl, cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"] + 99)
+        t0 = time.perf_counter()
+        po.track_fixed(f, s, p, dt, 1, nthreads=cores)
+        return time.perf_counter() - t0
+
+    n_cal, s_cal = 4 * cores * 64, 200
+    t_cal = run(n_cal, s_cal)
+    rate = n_cal * s_cal / t_cal
+    nsteps = 1000
+    nptl = int(max(cores * 64, min(cfg["nptl"], rate * target_s / nsteps)))
+    t = run(nptl, nsteps)
+    return {"value": nptl * nsteps / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d particles x %d steps of the same field and dt (oracle FP64, OpenMP %d threads)"
+                      % (nptl, nsteps, cores), "seconds": t}
+
+
+def reference_arm(args, world, rank):
+    """The reference's own CPU implementation of the path (its C restatement;
+    the reference tree itself is not on the GPU machine)."""
+    if rank != 0:
+        return
+    import test_particle_gb300 as tp
+    import test_particle_gb300.workloads as wl
+    cfg = wl.config_grid()
+    tp.lib().tp_init(0)
+    dom, grd, p0, he, hb = setup_grid(tp, wl, cfg, 0, to_host=True)
+    vals = []
+    base = None
+    for _ in range(max(1, args.steps)):
+        base = cpu_baseline(cfg, dom, grd, he, hb, target_s=8.0)
+        vals.append(base["value"])
+    v = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": cfg["name"], "particles_per_gpu": cfg["nptl"],
+                       "steps_per_run": cfg["steps"], "grid": [cfg["n"]] * 3},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": base["cores"], "kind": "port",
+                             "sample": base["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    args = ap.parse_args()
+    world, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+        return
+    import test_particle_gb300 as tp
+    import test_particle_gb300.workloads as wl
+    tp.check(tp.lib().tp_init(local), "tp_init")
+    cfg = wl.config_grid()
+    want_cpu = rank == 0 and world == 1 and not args.no_cpu_baseline
+    dom, grd, p0, he, hb = setup_grid(tp, wl, cfg, rank, to_host=want_cpu)
+    n = cfg["nptl"]
+    sess = tp.Session(n)
+    sess.load(p0)
+    dt, nt_out, nbins = cfg["dt"], cfg["nt_out"], cfg["nbins"]
+
+    # ---- mixed-precision path, particles resident in HBM
+    for _ in range(max(3, args.warmup)):
+        sess.track(dt, nt_out, nbins, tp.PREC_MIXED)
+    barrier(pg)
+    kms, sms, launches = [], [], 0
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            info = sess.track(dt, nt_out, nbins, tp.PREC_MIXED)
+            kms.append(info.kernel_ms)
+            sms.append(info.step_ms)
+            launches += info.launches
+        wall = time.perf_counter() - t0
+    barrier(pg)
+    dev_s = allmax(pg, sum(sms) / 1e3)
+    pushes = info.pushes
+    value = pushes * args.steps * world / dev_s
+    clocks = clk.summary()
+    diag = sess.fetch(nt_out, nbins, info.nsdc)
+
+    # ---- FP64 parity path on the same workload (fresh particle state)
+    sess.load(p0)
+    sess.track(dt, nt_out, nbins, tp.PREC_FP64)  # warm
+    f64 = []
+    for _ in range(max(1, args.fp64_steps)):
+        sess.load(p0)
+        f64.append(sess.track(dt, nt_out, nbins, tp.PREC_FP64).kernel_ms)
+    fp64_value = pushes / (float(np.median(f64)) / 1e3)
+    d64 = sess.fetch(nt_out, nbins, info.nsdc)
+    e1 = diag["espect"][-1] / max(1.0, diag["espect"][-1].sum())
+    e2 = d64["espect"][-1] / max(1.0, d64["espect"][-1].sum())
+    spec_l1 = float(np.abs(e1 - e2).sum())
+    dc_rel = np.abs(diag["dsum"][:, 1:] - d64["dsum"][:, 1:]) / np.maximum(np.abs(d64["dsum"][:, 1:]), 1e-300)
+    sess.close()
+
+    # ---- e2e: host buffers through the C ABI, copies inside the timed region
+    ptl = p0.copy()
+    e2e_times = []
+    import ctypes as C
+    L = tp.lib()
+    esp = np.zeros(nt_out * nbins)
+    ese = np.zeros(nt_out * nbins)
+    nsdc = info.nsdc
+    dsum = np.zeros(8 * nsdc)
+    rem = np.zeros(nsdc, dtype=np.int32)
+    nst = np.zeros(n, dtype=np.int32)
+    ri = tp.RunInfo()
+    for it in range(1 + args.steps):
+        t1 = time.perf_counter()
+        tp.check(L.tp_track_host(C.c_int(tp.PREC_MIXED), C.c_int(n), C.c_double(dt), C.c_int(nt_out),
+                                 C.c_int(nbins), tp._ptr(p0), tp._ptr(ptl), tp._ptr(nst), tp._ptr(esp),
+                                 tp._ptr(ese), tp._ptr(dsum), tp._ptr(rem), C.byref(ri)), "e2e")
+        if it > 0:
+            e2e_times.append(time.perf_counter() - t1)
+    e2e_s = allmax(pg, float(np.median(e2e_times)))
+    h2d = 2 * n * 88
+    d2h = n * 88 + n * 4 + 2 * nt_out * nbins * 4 + 8 * nsdc * 8 + nsdc * 4
+
+    hbm, peak_kind = peaks()
+    kernel_s = float(np.median(kms)) / 1e3
+    alg_bytes = pushes * 384.0  # 2 field evaluations x 8 corners x 6 FP32 components
+    achieved = alg_bytes / kernel_s / 1e9
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": dev_s * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Kolmogorov fields and particles)",
+            "config": {"workload": cfg["name"], "particles_per_gpu": n, "steps_per_run": cfg["steps"],
+                       "grid": [cfg["n"]] * 3, "field_bytes": cfg["n"] ** 3 * 32,
+                       "precision": "FP32 push/field, 64-bit fixed-point positions, FP64 sums",
+                       "l2": "inputs larger than L2 (4.3 GB field), no flush",
+                       "parallelism": "particles sharded, replicas of the field"},
+            "e2e": {"value": pushes * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+                         "kernel": "track_mixed_kernel<PIC>",
+                         "algorithmic_bytes_per_push": 384},
+            "fp64": {"value": fp64_value * world, "unit": UNIT,
+                     "mixed_over_fp64": value / (fp64_value * world),
+                     "spectrum_l1_mixed_vs_fp64": spec_l1,
+                     "diffusion_rel_err_mixed_vs_fp64_median": float(np.median(dc_rel))},
+            }
+    if want_cpu:
+        try:
+            line["cpu_baseline"] = cpu_baseline(cfg, dom, grd, he, hb)
+        except Exception as e:
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -205,8 +205,10 @@ typedef struct tp_session tp_session;
 typedef struct tp_run_info {
     int estep, einterval, nsdc, nt_out, nbins;
     int grid, blocks_per_sm;
-    double kernel_ms;          /* device time of the tracking kernel(s), CUDA events */
+    double kernel_ms;          /* device time of the tracking kernel, CUDA events */
     double pushes;             /* particle pushes performed */
+    double step_ms;            /* device time of the whole run incl. resets and reductions */
+    int launches;              /* kernels this library launched for the run */
 } tp_run_info;
 tp_session *tp_session_create(int nptl);
 void tp_session_destroy(tp_session *s);
@@ -215,6 +217,16 @@ int tp_session_track(tp_session *s, int precision, double dt, int nt_out, int nb
                      tp_run_info *info);
 int tp_session_fetch(tp_session *s, particles *ptl, int *nsteps_ptl,
                      double *espect, double *espect_escape, double *dsum, int *remain);
+
+/* Synthetic gridded fields (system type TP_SYS_PIC) generated on the GPU:
+ * B = B0z z + sum of modes_b, v = sum of modes_v, E = -v x B at every node of
+ * simul_grid, node (i,j,k) at phase 2 pi (n . (i/nx, j/ny, k/nz)) + phase.
+ * The device copies become authoritative; host_e / host_b (n*3 floats each,
+ * may be NULL) receive the same arrays.  tp_release_device_fields() returns
+ * to uploading the host arrays. */
+int tp_synth_pic_fields(int nmodes_b, const tp_mode *modes_b, int nmodes_v,
+                        const tp_mode *modes_v, double B0z, float *host_e, float *host_b);
+void tp_release_device_fields(void);
 
 /* One call, host buffers in and out (reuses a cached session). */
 int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,

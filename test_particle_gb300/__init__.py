@@ -53,7 +53,8 @@ class ParamFF(C.Structure):
 class RunInfo(C.Structure):
     _fields_ = [("estep", C.c_int), ("einterval", C.c_int), ("nsdc", C.c_int),
                 ("nt_out", C.c_int), ("nbins", C.c_int), ("grid", C.c_int),
-                ("blocks_per_sm", C.c_int), ("kernel_ms", C.c_double), ("pushes", C.c_double)]
+                ("blocks_per_sm", C.c_int), ("kernel_ms", C.c_double), ("pushes", C.c_double),
+                ("step_ms", C.c_double), ("launches", C.c_int)]
 
 
 def _copy_struct(dst_type, src):
@@ -237,6 +238,27 @@ def track(ptl_init, dt, nt_out, nbins, precision=PREC_FP64, ptl=None):
     return dict(ptl=p, estep=info.estep, espect=esp.reshape(nt_out, nbins),
                 espect_escape=ese.reshape(nt_out, nbins), dsum=dsum.reshape(8, nsdc),
                 remain=rem, nsteps=nst, info=info)
+
+
+def synth_pic_fields(modes_b, modes_v, B0z, to_host=False):
+    """Generate the PIC grids on the GPU for the current simul_grid; optionally
+    return the float AoS (E, B) arrays."""
+    L = lib()
+    mb = np.ascontiguousarray(modes_b, dtype=MODE_DTYPE)
+    mv = np.ascontiguousarray(modes_v, dtype=MODE_DTYPE)
+    he = hb = None
+    if to_host:
+        g = Grids.in_dll(L, "simul_grid")
+        n = g.nx * g.ny * g.nz
+        he = np.zeros((n, 3), dtype=np.float32)
+        hb = np.zeros((n, 3), dtype=np.float32)
+    check(L.tp_synth_pic_fields(C.c_int(len(mb)), _ptr(mb), C.c_int(len(mv)), _ptr(mv),
+                                C.c_double(B0z), _ptr(he), _ptr(hb)), "synth_pic_fields")
+    return he, hb
+
+
+def release_device_fields():
+    lib().tp_release_device_fields()
 
 
 def device_status():

@@ -22,10 +22,13 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcom
 UNITS = [
     ("track_fp64.o", "track_fp64.cu", ["-fmad=false"]),
     ("track_fp64fast.o", "track_fp64.cu", ["-fmad=true", "-DTP_FP64_NS=fp64fast"]),
+    ("track_mixed.o", "track_mixed.cu", ["-fmad=true"]),
+    ("mixed_host.o", "mixed_host.cu", []),
     ("capi.o", "capi.cu", []),
     ("session.o", "session.cu", []),
     ("ref_api.o", "ref_api.cu", []),
     ("bs.o", "bs.cu", []),
+    ("synth.o", "synth.cu", []),
     ("host_config.o", "host_config.cpp", ["-x", "cu"]),
 ]
 

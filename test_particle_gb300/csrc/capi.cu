@@ -106,6 +106,7 @@ bool Mirror::sync(const void* host, size_t b, cudaStream_t s)
     src = host;
     bytes = b;
     dirty = false;
+    g.upload_gen++;
     return true;
 }
 

@@ -6,6 +6,7 @@
 #include "../../include/tp_gpu.h"
 #include "tp_internal.h"
 #include "tp_kernels.h"
+#include "tp_kernels_mixed.h"
 #include "tp_session.h"
 
 namespace tp {
@@ -26,8 +27,8 @@ Session::~Session()
     for (Scratch* sc : {&soa, &soa0, &aos, &nsteps, &spec, &rem, &dpart, &dsum, &traj, &trajacc,
                         &trajpts})
         sc->release();
-    if (ev0) cudaEventDestroy(ev0);
-    if (ev1) cudaEventDestroy(ev1);
+    for (cudaEvent_t e : {ev0, ev1, evb, eve})
+        if (e) cudaEventDestroy(e);
 }
 
 bool Session::reserve(int n)
@@ -36,6 +37,8 @@ bool Session::reserve(int n)
     if (!ev0) {
         cudaEventCreate(&ev0);
         cudaEventCreate(&ev1);
+        cudaEventCreate(&evb);
+        cudaEventCreate(&eve);
     }
     if (n <= cap) return true;
     size_t rec = sizeof(double) * 11 * (size_t)n;
@@ -75,7 +78,14 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
         return false;
     }
     DevField f;
-    if (!build_field(system_type, f)) return false;
+    mixed::MixField mf;
+    int nmodes = 0;
+    const bool is_mixed = rs.precision == TP_PREC_MIXED;
+    if (is_mixed) {
+        if (!build_mixfield(system_type, mf, &nmodes)) return false;
+    } else if (!build_field(system_type, f)) {
+        return false;
+    }
     if (!ensure_thresholds(rs.nbins)) return false;
     cudaStream_t s = g.stream;
     nt_out = rs.nt_out;
@@ -85,6 +95,7 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
     int bps = 0;
     if (rs.precision == TP_PREC_FP64) bps = fp64::track_max_blocks_per_sm(system_type);
     else if (rs.precision == TP_PREC_FP64_FAST) bps = fp64fast::track_max_blocks_per_sm(system_type);
+    else if (is_mixed) bps = mixed::track_max_blocks_per_sm(system_type, nmodes);
     else {
         set_error(1, "precision %d not available for system type %d", rs.precision, system_type);
         return false;
@@ -99,6 +110,7 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
     double* d_dpart = (double*)dpart.get(sizeof(double) * 8 * (size_t)nsdc * grid);
     double* d_dsum = (double*)dsum.get(sizeof(double) * 8 * (size_t)nsdc);
     if (!d_spec || !d_rem || !d_dpart || !d_dsum) return false;
+    cudaEventRecord(evb, s);
     cudaMemsetAsync(d_spec, 0, sizeof(unsigned) * 2 * nspec, s);
     cudaMemsetAsync(d_rem, 0, sizeof(int) * nsdc, s);
     cudaMemsetAsync(d_dpart, 0, sizeof(double) * 8 * (size_t)nsdc * grid, s);
@@ -141,13 +153,16 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
     q.dt = rs.dt;
     cudaEventRecord(ev0, s);
     cudaError_t e = rs.precision == TP_PREC_FP64 ? fp64::launch_track(f, b, q, grid, s)
-                                                 : fp64fast::launch_track(f, b, q, grid, s);
+                  : is_mixed ? mixed::launch_track(mf, b, q, grid, s)
+                             : fp64fast::launch_track(f, b, q, grid, s);
     if (!cuda_ok(e, "track launch")) return false;
     cudaEventRecord(ev1, s);
     if (!cuda_ok(fp64::launch_reduce_dpart(d_dpart, grid, nsdc, d_dsum, s), "reduce")) return false;
+    cudaEventRecord(eve, s);
     if (!cuda_ok(cudaStreamSynchronize(s), "track")) return false;
-    float ms = 0.f;
+    float ms = 0.f, ms_step = 0.f;
     cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventElapsedTime(&ms_step, evb, eve);
     last_ms = ms;
     if (info) {
         info->estep = rs.estep;
@@ -158,6 +173,8 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
         info->grid = grid;
         info->blocks_per_sm = bps;
         info->kernel_ms = ms;
+        info->step_ms = ms_step;
+        info->launches = rs.reset_nsteps ? 3 : 2;
         info->pushes = (double)n * (rs.estep - rs.sstep + 1);
     }
     return true;

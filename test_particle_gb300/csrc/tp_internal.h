@@ -56,6 +56,13 @@ struct Ctx {
     double* d_thr = nullptr;
     // scratch for batch utilities
     Scratch s_batch_a, s_batch_b;
+    // mixed-precision field copies (FP32 node-interleaved grids, FP32 modes)
+    Scratch s_mix_v, s_mix_eb, s_mix_modes;
+    const float* eb_src_e = nullptr;
+    const float* eb_src_b = nullptr;
+    size_t eb_n = 0;
+    long eb_gen = -1;
+    long upload_gen = 0;     // bumped by every host-to-device field upload
 };
 
 extern Ctx g;
@@ -66,6 +73,8 @@ void die_if_error(const char* where);
 bool ensure_init();
 bool build_field(int stype, DevField& f);
 bool build_field_points(DevField& f);
+namespace mixed { struct MixField; }
+bool build_mixfield(int stype, mixed::MixField& mf, int* nmodes_out);
 const void* dd0(Mirror& m, const void* h, size_t b, cudaStream_t s);
 bool ensure_thresholds(int nbins);
 bool compute_thresholds(int nbins, double lmin, double lde, std::vector<double>& thr);

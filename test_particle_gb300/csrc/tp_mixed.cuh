@@ -1,0 +1,139 @@
+// tp_mixed.cuh -- FP32 field evaluation from 64-bit fixed-point positions.
+#pragma once
+#include "tp_common.cuh"
+
+namespace tp {
+namespace mixed {
+
+// One plane-wave mode in FP32 with its phase offset in 32-bit fixed point
+// (revolutions * 2^32).
+struct ModeF {
+    int n[3];
+    uint32_t ph;
+    float b[3];
+    float e[3];
+};
+
+struct MixField {
+    int system_type;
+    int bc_flag;
+    float cm;
+    double min[3], L[3];
+    float invL[3];
+    // ABC force-free field (src/force_free.c:138-150): B0 (A sin lz + C cos ly, ...)
+    float A, Bc, C, B0;
+    int abc_fixed;           // lambda * L / 2pi integral on every axis: exact fixed-point phase
+    uint32_t abc_m[3];       // lambda * L_k / 2pi
+    uint32_t abc_off[3];     // lambda * min_k / 2pi in revolutions * 2^32
+    float lam, lmin[3], lL[3];
+    // gridded fields: node-interleaved {E,0},{B,0} (PIC) or {v,0} (ABC velocity)
+    int nx, ny, nz;
+    int interp_ref;          // 1: the reference's weights (x and z fractions exchanged)
+    const float4* eb;
+    const float4* vgrid;
+    // plane-wave mode sum, B = mB0 z + sum
+    int nmodes;
+    const ModeF* modes;
+    float mB0;
+};
+
+__device__ __forceinline__ float rev_to_rad(uint32_t ph)
+{
+    return (float)(int32_t)ph * 1.46291807926715968e-9f;  // 2 pi / 2^32
+}
+
+// cell index and fraction along one axis from the top 32 bits of a position
+__device__ __forceinline__ void cell_of(uint64_t X, int n, int& i, float& fr)
+{
+    uint64_t G = (X >> 32) * (uint64_t)(uint32_t)(n - 1);
+    i = (int)(G >> 32);
+    fr = (float)(uint32_t)G * 2.3283064365386963e-10f;  // 2^-32
+}
+
+__device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t)
+{
+    return make_float4(fmaf(t, b.x - a.x, a.x), fmaf(t, b.y - a.y, a.y), fmaf(t, b.z - a.z, a.z), 0.f);
+}
+
+// trilinear interpolation of a node-interleaved field with `stride` float4s per node
+template <int STRIDE>
+__device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __restrict__ g,
+                                            const uint64_t X[3], float4 out[STRIDE])
+{
+    int ix, iy, iz;
+    float fx, fy, fz;
+    cell_of(X[0], f.nx, ix, fx);
+    cell_of(X[1], f.ny, iy, fy);
+    cell_of(X[2], f.nz, iz, fz);
+    if (f.interp_ref) {  // src/interpolation.c:173-180 pairs x weights with z corners
+        float t = fx;
+        fx = fz;
+        fz = t;
+    }
+    const size_t nx = f.nx, nxy = (size_t)f.nx * f.ny;
+    const size_t base = ix + nx * iy + nxy * iz;
+    const float4* p = g + base * STRIDE;
+#pragma unroll
+    for (int c = 0; c < STRIDE; c++) {
+        float4 c000 = __ldg(p + c), c100 = __ldg(p + STRIDE + c);
+        float4 c010 = __ldg(p + nx * STRIDE + c), c110 = __ldg(p + (nx + 1) * STRIDE + c);
+        float4 c001 = __ldg(p + nxy * STRIDE + c), c101 = __ldg(p + (nxy + 1) * STRIDE + c);
+        float4 c011 = __ldg(p + (nxy + nx) * STRIDE + c), c111 = __ldg(p + (nxy + nx + 1) * STRIDE + c);
+        float4 a = lerp4(c000, c100, fx), b = lerp4(c010, c110, fx);
+        float4 d = lerp4(c001, c101, fx), e = lerp4(c011, c111, fx);
+        out[c] = lerp4(lerp4(a, b, fy), lerp4(d, e, fy), fz);
+    }
+}
+
+template <int SYS>
+__device__ __forceinline__ void field_mixed(const MixField& f, const uint64_t X[3], float E[3],
+                                            float B[3], const ModeF* smodes)
+{
+    E[0] = E[1] = E[2] = 0.f;
+    if (SYS == TP_SYS_TEST) {
+        B[0] = 0.f; B[1] = 0.f; B[2] = 1.0f;
+    } else if (SYS == TP_SYS_FORCEFREE) {
+        float sx, cx, sy, cy, sz, cz;
+        if (f.abc_fixed) {
+            __sincosf(rev_to_rad((uint32_t)(X[0] >> 32) * f.abc_m[0] + f.abc_off[0]), &sx, &cx);
+            __sincosf(rev_to_rad((uint32_t)(X[1] >> 32) * f.abc_m[1] + f.abc_off[1]), &sy, &cy);
+            __sincosf(rev_to_rad((uint32_t)(X[2] >> 32) * f.abc_m[2] + f.abc_off[2]), &sz, &cz);
+        } else {
+            sincosf(f.lmin[0] + f.lL[0] * ((float)(X[0] >> 40) * 5.9604644775390625e-8f), &sx, &cx);
+            sincosf(f.lmin[1] + f.lL[1] * ((float)(X[1] >> 40) * 5.9604644775390625e-8f), &sy, &cy);
+            sincosf(f.lmin[2] + f.lL[2] * ((float)(X[2] >> 40) * 5.9604644775390625e-8f), &sz, &cz);
+        }
+        B[0] = f.B0 * (f.A * sz + f.C * cy);
+        B[1] = f.B0 * (f.Bc * sx + f.A * cz);
+        B[2] = f.B0 * (f.C * sy + f.Bc * cx);
+        if (f.vgrid) {  // E = -v x B, src/force_free.c:78-86
+            float4 v;
+            trilinear_f<1>(f, f.vgrid, X, &v);
+            E[0] = B[1] * v.z - B[2] * v.y;
+            E[1] = B[2] * v.x - B[0] * v.z;
+            E[2] = B[0] * v.y - B[1] * v.x;
+        }
+    } else if (SYS == TP_SYS_PIC) {
+        float4 eb[2];
+        trilinear_f<2>(f, f.eb, X, eb);
+        E[0] = eb[0].x; E[1] = eb[0].y; E[2] = eb[0].z;
+        B[0] = eb[1].x; B[1] = eb[1].y; B[2] = eb[1].z;
+    } else if (SYS == TP_SYS_MODESUM) {
+        const uint32_t X32 = (uint32_t)(X[0] >> 32), Y32 = (uint32_t)(X[1] >> 32),
+                       Z32 = (uint32_t)(X[2] >> 32);
+        float b0 = 0.f, b1 = 0.f, b2 = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f;
+#pragma unroll 4
+        for (int m = 0; m < f.nmodes; m++) {
+            const ModeF& md = smodes[m];
+            uint32_t ph = (uint32_t)md.n[0] * X32 + (uint32_t)md.n[1] * Y32 + (uint32_t)md.n[2] * Z32 + md.ph;
+            float c = __cosf(rev_to_rad(ph));
+            b0 = fmaf(md.b[0], c, b0); b1 = fmaf(md.b[1], c, b1); b2 = fmaf(md.b[2], c, b2);
+            e0 = fmaf(md.e[0], c, e0); e1 = fmaf(md.e[1], c, e1); e2 = fmaf(md.e[2], c, e2);
+        }
+        B[0] = b0; B[1] = b1; B[2] = f.mB0 + b2;
+        E[0] = e0; E[1] = e1; E[2] = e2;
+    }
+}
+
+}  // namespace mixed
+}  // namespace tp

@@ -27,7 +27,7 @@ struct Session {
     Scratch traj, trajacc, trajpts;
     long traj_total = 0;
     int nt_out = 0, nbins = 0, nsdc = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evb = nullptr, eve = nullptr;
     float last_ms = 0.f;
     ~Session();
     bool reserve(int n);
