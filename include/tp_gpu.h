@@ -228,6 +228,24 @@ int tp_synth_pic_fields(int nmodes_b, const tp_mode *modes_b, int nmodes_v,
                         const tp_mode *modes_v, double B0z, float *host_e, float *host_b);
 void tp_release_device_fields(void);
 
+/* Adaptive Bulirsch-Stoer (src/unused/StepperBS.c) for the wire-loop field
+ * (system type 1), batched on the GPU.  y: n * 6 doubles, (x, y, z, beta)
+ * for uform 0 (the reference's equations, positions in L0, c0/L0 scaling)
+ * or (x, y, z, u = gamma v) for uform 1 (c = 1).
+ * tp_bs_steps: exactly nsteps accepted steps from t0 with first step h0;
+ * rec receives (t, h, y[6]) per particle and step (n * nsteps * 8).
+ * tp_bs_run: from t[i] to t_end with step sizes clipped to land on the
+ * nt_out frame times, where the energy spectrum (nt_out * nbins counts) and
+ * the diffusion sums (dframe: (nt_out + 1) * 8, row f + 1 = frame f) are
+ * taken; steps_out / status_out per particle (status: TP step limit 4,
+ * step-size underflow 8, non-finite state 2). */
+int tp_bs_steps(int n, double *y, double t0, double h0, int nsteps, double atol,
+                double rtol, int kmaxx, int uform, double *rec);
+int tp_bs_run(int n, double *y, double *t, double t_end, int nt_out, int nbins,
+              double h0, double atol, double rtol, int kmaxx, int uform, int max_steps,
+              int *steps_out, int *status_out, double *espect, double *dframe,
+              tp_run_info *info);
+
 /* One call, host buffers in and out (reuses a cached session). */
 int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,
                   const particles *ptl_init, particles *ptl, int *nsteps_ptl,

@@ -422,9 +422,14 @@ extern "C" void tp_set_spectrum(int nbins, double e_min, double e_max)
     logde = (logemax - logemin) / (nbins - 2);
 }
 
+// The host arrays are authoritative again: device-only copies (synthesised
+// fields) are dropped and everything is re-uploaded at the next use.
 extern "C" void tp_mark_fields_dirty(void)
 {
-    for (Mirror* m : g.all_mirrors()) m->dirty = true;
+    for (Mirror* m : g.all_mirrors()) {
+        if (m->device_only) m->release();
+        m->dirty = true;
+    }
 }
 
 extern "C" int tp_energy_thresholds(int nbins, double* thr)

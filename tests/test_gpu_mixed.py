@@ -42,20 +42,24 @@ def setup(kind, steps, n=8192, seed=5):
 
 
 @pytest.mark.parametrize("kind", ["abc", "grid", "modesum"])
-def test_mixed_short_horizon_per_particle(kind):
-    cfg, p0 = setup(kind, 200)
-    a = tp.track(p0, cfg["dt"], 2, 200, precision=tp.PREC_FP64)
-    b = tp.track(p0, cfg["dt"], 2, 200, precision=tp.PREC_MIXED)
+@pytest.mark.parametrize("steps,tol", [(1, 1e-5), (10, 1e-4)])
+def test_mixed_short_horizon_per_particle(kind, steps, tol):
+    """Before chaos amplifies FP32 rounding (the mode-sum field decorrelates
+    within a few tens of steps) each particle follows the FP64 path."""
+    cfg, p0 = setup(kind, steps)
+    a = tp.track(p0, cfg["dt"], 1, 200, precision=tp.PREC_FP64)
+    b = tp.track(p0, cfg["dt"], 1, 200, precision=tp.PREC_MIXED)
     L = np.array(cfg["hi"]) - np.array(cfg["lo"])
+    u_a = np.sqrt(a["ptl"]["ux"] ** 2 + a["ptl"]["uy"] ** 2 + a["ptl"]["uz"] ** 2)
     for k, ax in (("x", 0), ("y", 1), ("z", 2)):
         pa = a["ptl"][k] + a["ptl"][k + "shift"]
         pb = b["ptl"][k] + b["ptl"][k + "shift"]
-        err = np.abs(pa - pb) / L[ax]
-        assert np.median(err) < 1e-4, (k, np.median(err))
-    u_a = np.sqrt(a["ptl"]["ux"] ** 2 + a["ptl"]["uy"] ** 2 + a["ptl"]["uz"] ** 2)
-    u_b = np.sqrt(b["ptl"]["ux"] ** 2 + b["ptl"]["uy"] ** 2 + b["ptl"]["uz"] ** 2)
-    assert np.median(np.abs(u_a - u_b) / u_a) < 1e-4
-    np.testing.assert_allclose(b["dsum"][:, 1:], a["dsum"][:, 1:], rtol=2e-2)
+        disp = np.abs(pa - p0[k]) + 1e-3 * L[ax]
+        assert np.median(np.abs(pa - pb) / disp) < tol, k
+        uk = "u" + k
+        assert np.median(np.abs(a["ptl"][uk] - b["ptl"][uk]) / u_a) < tol, uk
+    assert np.array_equal(a["ptl"]["t"], p0["t"] + steps * cfg["dt"]) or \
+        np.allclose(b["ptl"]["t"], a["ptl"]["t"], rtol=1e-14)
     assert tp.device_status() == 0
 
 
@@ -70,7 +74,9 @@ def test_mixed_long_horizon_statistics(kind):
     l1 = np.abs(sa - sb).sum(axis=1)
     # statistical noise floor of two decorrelated ensembles of n particles
     assert np.all(l1 < 0.15), l1
-    rel = np.abs(b["dsum"][:, 1:] - a["dsum"][:, 1:]) / np.abs(a["dsum"][:, 1:]).max(axis=1, keepdims=True)
+    scale = np.abs(a["dsum"][:, 1:]).max(axis=1, keepdims=True)
+    live = scale[:, 0] > 1e-12  # rows that are not rounding noise (dee with E = 0)
+    rel = np.abs(b["dsum"][live, 1:] - a["dsum"][live, 1:]) / scale[live]
     assert np.median(rel) < 0.1
     assert tp.device_status() == 0
 
