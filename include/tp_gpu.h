@@ -177,7 +177,7 @@ int tp_init(int device);              /* select the GPU; implicit on first use *
 int tp_last_status(void);             /* 0 = ok; sticky until tp_clear_status() */
 const char *tp_last_error(void);
 void tp_clear_status(void);
-int tp_device_status(void);           /* status bits raised by kernels (bounds, limits) */
+int tp_device_status(void);           /* status bits raised by kernels since the last call (read and cleared) */
 
 /* Reference compile-time choices made run-time switches. */
 void tp_set_abc(double A, double B, double C);   /* include/force_free.h:21-26 */

@@ -119,9 +119,9 @@ struct Ctrl {
 // step, src/unused/StepperBS.c:159-354 without dense output; as in the
 // reference's StepperBS (:77-83) each step starts from the initial k_targ.
 // Returns 0, or ST_STEP_LIMIT when the rejection cap is hit.
-__device__ int bs_step(const DevField& f, int uform, int max_rejects, double& x, double* y,
-                       double* dydx, double htry, double hnext_in, Ctrl& c, double& hdid,
-                       double& hnext_out, int* status)
+__device__ int bs_step(const DevField& f, int uform, int max_rejects, bool nan_rejects, double& x,
+                       double* y, double* dydx, double htry, double hnext_in, Ctrl& c,
+                       double& hdid, double& hnext_out, int* status)
 {
     const double STEPFAC1 = 0.65, STEPFAC2 = 0.94, STEPFAC3 = 0.02, STEPFAC4 = 4.0;
     const double KFAC1 = 0.8, KFAC2 = 0.9;
@@ -165,6 +165,14 @@ __device__ int bs_step(const DevField& f, int uform, int max_rejects, double& x,
                     err += pow((y[i] - table[0][i]) / scale, 2.0);
                 }
                 err = sqrt(err / kNv);
+                if (nan_rejects && !(err == err)) {
+                    // a trial that left the domain of the equations (|beta| >= 1):
+                    // reject and retry a quarter of the step; the reference
+                    // accepts it because every comparison with NaN is false
+                    c.reject = true;
+                    hnew = 0.25 * fabs(h);
+                    break;
+                }
                 double expo = 1.0 / (2 * k + 1);
                 double facmin = pow(STEPFAC3, expo);
                 if (err == 0.0) {
@@ -275,7 +283,7 @@ __global__ void bs_steps_kernel(DevField f, BsArgs a)
     derivs(f, a.uform, x, y, dydx, a.status);
     int st = 0;
     for (int s = 0; s < a.nsteps && st == 0; s++) {
-        st = bs_step(f, a.uform, a.max_rejects, x, y, dydx, h, h, c, hdid, hnext, a.status);
+        st = bs_step(f, a.uform, a.max_rejects, false, x, y, dydx, h, h, c, hdid, hnext, a.status);
         double* r = a.rec + ((size_t)i * a.nsteps + s) * 8;
         r[0] = x;
         r[1] = hdid;
@@ -325,7 +333,7 @@ __global__ void __launch_bounds__(128) bs_track_kernel(DevField f, BsArgs a)
                 break;
             }
             double hn;
-            st = bs_step(f, a.uform, a.max_rejects, x, y, dydx, htry, hprev, c, hdid, hn, a.status);
+            st = bs_step(f, a.uform, a.max_rejects, true, x, y, dydx, htry, hprev, c, hdid, hn, a.status);
             if (st) break;
             nacc++;
             hnext = clip ? fmax(hn, hprev) : hn;

@@ -378,11 +378,13 @@ extern "C" void tp_clear_status(void)
     g.err[0] = 0;
 }
 
+// Status bits raised by kernels since the last call (read and cleared).
 extern "C" int tp_device_status(void)
 {
     if (!ensure_init()) return -1;
     int h = 0;
     cudaMemcpyAsync(&h, g.d_status, sizeof(int), cudaMemcpyDeviceToHost, g.stream);
+    cudaMemsetAsync(g.d_status, 0, sizeof(int), g.stream);
     cudaStreamSynchronize(g.stream);
     return h;
 }

@@ -55,10 +55,20 @@ __device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t)
     return make_float4(fmaf(t, b.x - a.x, a.x), fmaf(t, b.y - a.y, a.y), fmaf(t, b.z - a.z, a.z), 0.f);
 }
 
+// The eight corner nodes of the cell a particle last sampled, kept in
+// registers: at a few tenths of a cell per step most evaluations fall in the
+// same cell as the previous one and need no memory traffic at all.
+template <int STRIDE>
+struct CellCache {
+    long long key = -1;
+    float4 c[8 * STRIDE];
+};
+
 // trilinear interpolation of a node-interleaved field with `stride` float4s per node
 template <int STRIDE>
 __device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __restrict__ g,
-                                            const uint64_t X[3], float4 out[STRIDE])
+                                            const uint64_t X[3], CellCache<STRIDE>& cc,
+                                            float4 out[STRIDE])
 {
     int ix, iy, iz;
     float fx, fy, fz;
@@ -70,24 +80,42 @@ __device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __r
         fx = fz;
         fz = t;
     }
-    const size_t nx = f.nx, nxy = (size_t)f.nx * f.ny;
-    const size_t base = ix + nx * iy + nxy * iz;
-    const float4* p = g + base * STRIDE;
+    const long long nx = f.nx, nxy = (long long)f.nx * f.ny;
+    const long long base = ix + nx * iy + nxy * iz;
+    if (base != cc.key) {
+        const float4* p = g + base * STRIDE;
+#pragma unroll
+        for (int c = 0; c < STRIDE; c++) {
+            cc.c[0 * STRIDE + c] = __ldg(p + c);
+            cc.c[1 * STRIDE + c] = __ldg(p + STRIDE + c);
+            cc.c[2 * STRIDE + c] = __ldg(p + nx * STRIDE + c);
+            cc.c[3 * STRIDE + c] = __ldg(p + (nx + 1) * STRIDE + c);
+            cc.c[4 * STRIDE + c] = __ldg(p + nxy * STRIDE + c);
+            cc.c[5 * STRIDE + c] = __ldg(p + (nxy + 1) * STRIDE + c);
+            cc.c[6 * STRIDE + c] = __ldg(p + (nxy + nx) * STRIDE + c);
+            cc.c[7 * STRIDE + c] = __ldg(p + (nxy + nx + 1) * STRIDE + c);
+        }
+        cc.key = base;
+    }
 #pragma unroll
     for (int c = 0; c < STRIDE; c++) {
-        float4 c000 = __ldg(p + c), c100 = __ldg(p + STRIDE + c);
-        float4 c010 = __ldg(p + nx * STRIDE + c), c110 = __ldg(p + (nx + 1) * STRIDE + c);
-        float4 c001 = __ldg(p + nxy * STRIDE + c), c101 = __ldg(p + (nxy + 1) * STRIDE + c);
-        float4 c011 = __ldg(p + (nxy + nx) * STRIDE + c), c111 = __ldg(p + (nxy + nx + 1) * STRIDE + c);
-        float4 a = lerp4(c000, c100, fx), b = lerp4(c010, c110, fx);
-        float4 d = lerp4(c001, c101, fx), e = lerp4(c011, c111, fx);
+        float4 a = lerp4(cc.c[0 * STRIDE + c], cc.c[1 * STRIDE + c], fx);
+        float4 b = lerp4(cc.c[2 * STRIDE + c], cc.c[3 * STRIDE + c], fx);
+        float4 d = lerp4(cc.c[4 * STRIDE + c], cc.c[5 * STRIDE + c], fx);
+        float4 e = lerp4(cc.c[6 * STRIDE + c], cc.c[7 * STRIDE + c], fx);
         out[c] = lerp4(lerp4(a, b, fy), lerp4(d, e, fy), fz);
     }
 }
 
+// Per-particle register state of the field evaluation.
+struct FieldCache {
+    CellCache<2> eb;   // gridded E, B
+    CellCache<1> v;    // ABC velocity grid
+};
+
 template <int SYS>
 __device__ __forceinline__ void field_mixed(const MixField& f, const uint64_t X[3], float E[3],
-                                            float B[3], const ModeF* smodes)
+                                            float B[3], const ModeF* smodes, FieldCache& fc)
 {
     E[0] = E[1] = E[2] = 0.f;
     if (SYS == TP_SYS_TEST) {
@@ -108,14 +136,14 @@ __device__ __forceinline__ void field_mixed(const MixField& f, const uint64_t X[
         B[2] = f.B0 * (f.C * sy + f.Bc * cx);
         if (f.vgrid) {  // E = -v x B, src/force_free.c:78-86
             float4 v;
-            trilinear_f<1>(f, f.vgrid, X, &v);
+            trilinear_f<1>(f, f.vgrid, X, fc.v, &v);
             E[0] = B[1] * v.z - B[2] * v.y;
             E[1] = B[2] * v.x - B[0] * v.z;
             E[2] = B[0] * v.y - B[1] * v.x;
         }
     } else if (SYS == TP_SYS_PIC) {
         float4 eb[2];
-        trilinear_f<2>(f, f.eb, X, eb);
+        trilinear_f<2>(f, f.eb, X, fc.eb, eb);
         E[0] = eb[0].x; E[1] = eb[0].y; E[2] = eb[0].z;
         B[0] = eb[1].x; B[1] = eb[1].y; B[2] = eb[1].z;
     } else if (SYS == TP_SYS_MODESUM) {

@@ -47,11 +47,11 @@ __device__ __forceinline__ void advance(uint64_t& X, int& img, float fr)
 
 template <int SYS>
 __device__ __forceinline__ void wirz_mixed(const MixField& f, PM& p, float dt, const ModeF* smodes,
-                                           bool& escaped)
+                                           FieldCache& fc, bool& escaped)
 {
     const float cm = f.cm;
     float E[3], B[3];
-    field_mixed<SYS>(f, p.X, E, B, smodes);
+    field_mixed<SYS>(f, p.X, E, B, smodes, fc);
     float Btot = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
     float iB = 1.0f / Btot;
     float h[3] = {B[0] * iB, B[1] * iB, B[2] * iB};
@@ -78,7 +78,7 @@ __device__ __forceinline__ void wirz_mixed(const MixField& f, PM& p, float dt, c
     uint64_t Xp[3] = {p.X[0], p.X[1], p.X[2]};
 #pragma unroll
     for (int k = 0; k < 3; k++) Xp[k] += (uint64_t)float_to_fx(dpre[k]);
-    field_mixed<SYS>(f, Xp, E, B, smodes);
+    field_mixed<SYS>(f, Xp, E, B, smodes, fc);
     Btot = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
     iB = 1.0f / Btot;
     h[0] = B[0] * iB; h[1] = B[1] * iB; h[2] = B[2] * iB;
@@ -133,10 +133,10 @@ __device__ __forceinline__ int energy_bin_f(const double* thr, int nbins, const 
 // pitch-angle cosine of u against the local field, FP32 field, returned in double
 template <int SYS>
 __device__ __forceinline__ double pitch_mu(const MixField& f, const uint64_t X[3], const float u[3],
-                                           const ModeF* smodes)
+                                           const ModeF* smodes, FieldCache& fc)
 {
     float E[3], B[3];
-    field_mixed<SYS>(f, X, E, B, smodes);
+    field_mixed<SYS>(f, X, E, B, smodes, fc);
     float bb = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
     float uu = sqrtf(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
     return (double)((B[0] * u[0] + B[1] * u[1] + B[2] * u[2]) / (bb * uu));
@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(kBlock) track_mixed_kernel(MixField f, TrackBu
         const int i = tile * kBlock + threadIdx.x;
         const bool active = i < q.n;
         PM p = {};
+        FieldCache fc;
         double x0[3] = {0, 0, 0}, u0[3] = {0, 0, 0}, tstart = 0.0, mu0 = 0.0;
         int nst = 1;
         bool esc = false;
@@ -208,7 +209,7 @@ __global__ void __launch_bounds__(kBlock) track_mixed_kernel(MixField f, TrackBu
                 double r = (x0[k] - f.min[k]) / f.L[k];
                 X0[k] = __double2ull_rz((r - floor(r)) * 18446744073709551616.0);
             }
-            mu0 = pitch_mu<SYS>(f, X0, uf0, smodes);
+            mu0 = pitch_mu<SYS>(f, X0, uf0, smodes, fc);
         }
         int esc_pre = esc ? 1 : 0;
         int esc_after = esc_pre;
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(kBlock) track_mixed_kernel(MixField f, TrackBu
             sg[0] = 0.0; sg[4] = 0.0; sg[5] = 0.0;
             if (active && (esc_pre == 0 || f.bc_flag == 0)) {
                 bool e2 = false;
-                wirz_mixed<SYS>(f, p, dt, smodes, e2);
+                wirz_mixed<SYS>(f, p, dt, smodes, fc, e2);
                 if (e2) esc_after = 1;
                 nst += 1;
                 done += 1;
@@ -239,7 +240,7 @@ __global__ void __launch_bounds__(kBlock) track_mixed_kernel(MixField f, TrackBu
                     double du0 = u0[0] - p.u[0], du1 = u0[1] - p.u[1], du2 = u0[2] - p.u[2];
                     double g1 = sqrt(1.0 + (double)p.u[0] * p.u[0] + (double)p.u[1] * p.u[1] + (double)p.u[2] * p.u[2]);
                     double g0 = sqrt(1.0 + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
-                    double mu = pitch_mu<SYS>(f, p.X, p.u, smodes);
+                    double mu = pitch_mu<SYS>(f, p.X, p.u, smodes, fc);
                     double th = (double)acosf((float)mu) * (180.0 / 3.14159265358979323846);
                     double th0 = (double)acosf((float)mu0) * (180.0 / 3.14159265358979323846);
                     sg[1] = dxx; sg[2] = dyy; sg[3] = dzz;
