@@ -246,6 +246,25 @@ int tp_bs_run(int n, double *y, double *t, double t_end, int nt_out, int nbins,
               int *steps_out, int *status_out, double *espect, double *dframe,
               tp_run_info *info);
 
+/* Learned field model (no reference counterpart): 64 integer-lattice Fourier
+ * features of the box position, then 128 -> 256 -> 256 -> 256 -> 256 -> 6
+ * with SiLU, BF16 tensor-core GEMMs with FP32 accumulation, trained with
+ * AdamW on samples of the current plane-wave mode table (tp_set_modes).
+ * Parameters are one flat FP32 array W0, b0, ..., W4, b4 (W_l [out][in]).
+ * Positions u are box fractions in 32-bit fixed point (u * 2^32). */
+int tp_mlp_param_count(void);
+int tp_mlp_init(const int *freq /* 64 x 3 */, const float *weights /* NULL: seeded init */,
+                unsigned long long seed);
+int tp_mlp_set_output_norm(const float *mean6, const float *std6);
+int tp_mlp_get_weights(float *weights);
+int tp_mlp_grad(int n, const unsigned int *u, const float *t, double *loss, float *y,
+                float *grads);
+int tp_mlp_train(long long nsamples, int batch, int epochs, double lr, double wd,
+                 unsigned long long seed, double *loss_out, double *ms_out);
+int tp_mlp_eval(int n, const unsigned int *u, float *out6);
+/* Same, through the block-wide evaluation the tracking kernel uses. */
+int tp_mlp_eval_kernel(int n, const unsigned int *u, float *out6);
+
 /* One call, host buffers in and out (reuses a cached session). */
 int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,
                   const particles *ptl_init, particles *ptl, int *nsteps_ptl,

@@ -261,6 +261,62 @@ def release_device_fields():
     lib().tp_release_device_fields()
 
 
+# ---------------------------------------------------------------- learned field model
+def mlp_param_count():
+    return lib().tp_mlp_param_count()
+
+
+def mlp_init(freq, weights=None, seed=1):
+    f = np.ascontiguousarray(freq, dtype=np.int32).reshape(64, 3)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+    check(lib().tp_mlp_init(_ptr(f), _ptr(w), C.c_ulonglong(seed)), "mlp_init")
+
+
+def mlp_set_output_norm(mean, std):
+    m = np.ascontiguousarray(mean, dtype=np.float32)
+    s = np.ascontiguousarray(std, dtype=np.float32)
+    check(lib().tp_mlp_set_output_norm(_ptr(m), _ptr(s)), "mlp_set_output_norm")
+
+
+def mlp_weights():
+    w = np.zeros(mlp_param_count(), dtype=np.float32)
+    check(lib().tp_mlp_get_weights(_ptr(w)), "mlp_get_weights")
+    return w
+
+
+def mlp_grad(u, t):
+    u = np.ascontiguousarray(u, dtype=np.uint32).reshape(-1, 3)
+    t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, 6)
+    n = len(u)
+    loss = C.c_double()
+    y = np.zeros((n, 6), dtype=np.float32)
+    g = np.zeros(mlp_param_count(), dtype=np.float32)
+    check(lib().tp_mlp_grad(C.c_int(n), _ptr(u), _ptr(t), C.byref(loss), _ptr(y), _ptr(g)), "mlp_grad")
+    return loss.value, y, g
+
+
+def mlp_train(nsamples, batch, epochs, lr=2e-3, wd=0.0, seed=7):
+    loss, ms = C.c_double(), C.c_double()
+    check(lib().tp_mlp_train(C.c_longlong(nsamples), C.c_int(batch), C.c_int(epochs), C.c_double(lr),
+                             C.c_double(wd), C.c_ulonglong(seed), C.byref(loss), C.byref(ms)),
+          "mlp_train")
+    return loss.value, ms.value
+
+
+def mlp_eval(u):
+    u = np.ascontiguousarray(u, dtype=np.uint32).reshape(-1, 3)
+    out = np.zeros((len(u), 6), dtype=np.float32)
+    check(lib().tp_mlp_eval(C.c_int(len(u)), _ptr(u), _ptr(out)), "mlp_eval")
+    return out
+
+
+def mlp_eval_kernel(u):
+    u = np.ascontiguousarray(u, dtype=np.uint32).reshape(-1, 3)
+    out = np.zeros((len(u), 6), dtype=np.float32)
+    check(lib().tp_mlp_eval_kernel(C.c_int(len(u)), _ptr(u), _ptr(out)), "mlp_eval_kernel")
+    return out
+
+
 def device_status():
     return lib().tp_device_status()
 

@@ -29,6 +29,8 @@ UNITS = [
     ("ref_api.o", "ref_api.cu", []),
     ("bs.o", "bs.cu", []),
     ("synth.o", "synth.cu", []),
+    ("mlp.o", "mlp.cu", []),
+    ("track_surrogate.o", "track_surrogate.cu", ["-fmad=true"]),
     ("host_config.o", "host_config.cpp", ["-x", "cu"]),
 ]
 

@@ -1,0 +1,716 @@
+// mlp.cu -- training and inference of the learned field model on the tensor
+// cores: a tiled BF16 GEMM (mma.sync m16n8k16, FP32 accumulation) with fused
+// bias/SiLU epilogues, Fourier features, MSE loss, AdamW.
+//
+// The model maps a position u in the periodic box (u = (x - min) / L) to the
+// six field components: 64 integer-lattice frequencies f_j give the features
+// sin(2 pi f_j . u), cos(2 pi f_j . u) (exact phases in 32-bit fixed point),
+// then 128 -> 256 -> 256 -> 256 -> 256 -> 6 with SiLU.  Outputs are trained
+// on normalised components (zero mean, unit variance per component).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/tp_gpu.h"
+#include "mlp_common.cuh"
+#include "tp_internal.h"
+#include "tp_mixed.cuh"
+
+namespace tp {
+namespace mlp {
+
+// ---------------------------------------------------------------- GEMM
+// C[m][n] = sum_k A(m, k) * B(n, k); A(m, k) = A[m * lda + k] (or A[k * lda + m]
+// with AT), B(n, k) = B[n * ldb + k] (or B[k * ldb + n] with BT).  Block tile
+// 128 x 128 x 32, 8 warps as 4 (m) x 2 (n), each warp 32 x 64.
+constexpr int TM = 128, TN = 128, TK = 32, TKP = TK + 8;
+
+template <bool AT, bool BT, class Epi>
+__global__ void __launch_bounds__(256) gemm_kernel(const __nv_bfloat16* __restrict__ A, int lda,
+                                                   const __nv_bfloat16* __restrict__ B, int ldb,
+                                                   int M, int N, int K, int kchunk, Epi epi)
+{
+    __shared__ __align__(16) __nv_bfloat16 As[TM][TKP];
+    __shared__ __align__(16) __nv_bfloat16 Bs[TN][TKP];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp & 3, wn = warp >> 2;
+    const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
+    const int kbeg = blockIdx.z * kchunk;
+    const int kend = min(K, kbeg + kchunk);
+    const int g = lane >> 2, t = lane & 3;
+    float acc[2][8][4];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
+    const __nv_bfloat16 zero = __float2bfloat16(0.f);
+
+    for (int k0 = kbeg; k0 < kend; k0 += TK) {
+        // ---- stage A and B tiles (canonical [row][k] layouts)
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            int c = tid + r * 256;  // 512 chunks of 8 elements
+            if (!AT) {
+                int row = c >> 2, kk = (c & 3) * 8;
+                int m = m0 + row;
+#pragma unroll
+                for (int e = 0; e < 8; e++) {
+                    int k = k0 + kk + e;
+                    As[row][kk + e] = (m < M && k < kend) ? A[(size_t)m * lda + k] : zero;
+                }
+            } else {
+                int kr = c >> 4, mm = (c & 15) * 8;
+                int k = k0 + kr;
+#pragma unroll
+                for (int e = 0; e < 8; e++) {
+                    int m = m0 + mm + e;
+                    As[mm + e][kr] = (m < M && k < kend) ? A[(size_t)k * lda + m] : zero;
+                }
+            }
+            if (!BT) {
+                int row = c >> 2, kk = (c & 3) * 8;
+                int n = n0 + row;
+#pragma unroll
+                for (int e = 0; e < 8; e++) {
+                    int k = k0 + kk + e;
+                    Bs[row][kk + e] = (n < N && k < kend) ? B[(size_t)n * ldb + k] : zero;
+                }
+            } else {
+                int kr = c >> 4, nn = (c & 15) * 8;
+                int k = k0 + kr;
+#pragma unroll
+                for (int e = 0; e < 8; e++) {
+                    int n = n0 + nn + e;
+                    Bs[nn + e][kr] = (n < N && k < kend) ? B[(size_t)k * ldb + n] : zero;
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < TK; ks += 16) {
+            uint32_t af[2][4], bf[8][2];
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                int r = wm * 32 + i * 16 + g;
+                af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t]);
+                af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t]);
+                af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t + 8]);
+                af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                int r = wn * 64 + j * 8 + g;
+                bf[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[r][ks + 2 * t]);
+                bf[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[r][ks + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; i++)
+#pragma unroll
+                for (int j = 0; j < 8; j++) mma_bf16(acc[i][j], af[i], bf[j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            int m = m0 + wm * 32 + i * 16 + g;
+            int n = n0 + wn * 64 + j * 8 + 2 * t;
+            epi(m, n, acc[i][j][0], acc[i][j][1], M, N);
+            epi(m + 8, n, acc[i][j][2], acc[i][j][3], M, N);
+        }
+}
+
+// z = acc + b; Z <- bf16(z) (kept for the backward pass), H <- bf16(silu(z))
+struct EpiHidden {
+    const float* b;
+    __nv_bfloat16* Z;
+    __nv_bfloat16* H;
+    int ld;
+    __device__ void operator()(int m, int n, float v0, float v1, int M, int N) const
+    {
+        if (m >= M) return;
+        if (n < N) {
+            float z = v0 + b[n];
+            Z[(size_t)m * ld + n] = __float2bfloat16(z);
+            H[(size_t)m * ld + n] = __float2bfloat16(silu(z));
+        }
+        if (n + 1 < N) {
+            float z = v1 + b[n + 1];
+            Z[(size_t)m * ld + n + 1] = __float2bfloat16(z);
+            H[(size_t)m * ld + n + 1] = __float2bfloat16(silu(z));
+        }
+    }
+};
+
+// y = acc + b (FP32 output layer)
+struct EpiOut {
+    const float* b;
+    float* Y;
+    int ld;
+    __device__ void operator()(int m, int n, float v0, float v1, int M, int N) const
+    {
+        if (m >= M) return;
+        if (n < N) Y[(size_t)m * ld + n] = v0 + b[n];
+        if (n + 1 < N) Y[(size_t)m * ld + n + 1] = v1 + b[n + 1];
+    }
+};
+
+// dZ = dH * silu'(Z), stored BF16
+struct EpiBackSilu {
+    const __nv_bfloat16* Z;
+    __nv_bfloat16* G;
+    int ld;
+    __device__ void operator()(int m, int n, float v0, float v1, int M, int N) const
+    {
+        if (m >= M) return;
+        if (n < N) G[(size_t)m * ld + n] = __float2bfloat16(v0 * silu_grad(__bfloat162float(Z[(size_t)m * ld + n])));
+        if (n + 1 < N)
+            G[(size_t)m * ld + n + 1] =
+                __float2bfloat16(v1 * silu_grad(__bfloat162float(Z[(size_t)m * ld + n + 1])));
+    }
+};
+
+// FP32 accumulation of a split-K weight gradient
+struct EpiAtomic {
+    float* W;
+    int ld;
+    __device__ void operator()(int m, int n, float v0, float v1, int M, int N) const
+    {
+        if (m >= M) return;
+        if (n < N) atomicAdd(&W[(size_t)m * ld + n], v0);
+        if (n + 1 < N) atomicAdd(&W[(size_t)m * ld + n + 1], v1);
+    }
+};
+
+template <bool AT, bool BT, class Epi>
+static cudaError_t gemm(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M,
+                        int N, int K, int splits, Epi epi, cudaStream_t s)
+{
+    int kchunk = (K + splits - 1) / splits;
+    kchunk = (kchunk + TK - 1) / TK * TK;
+    splits = (K + kchunk - 1) / kchunk;
+    dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, splits);
+    gemm_kernel<AT, BT, Epi><<<grid, 256, 0, s>>>(A, lda, B, ldb, M, N, K, kchunk, epi);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- features
+// X[b][j] = sin(2 pi f_j . u_b), X[b][64 + j] = cos(...); u as 32-bit fixed point
+__device__ __forceinline__ void features_row(const int* freq, uint32_t U0, uint32_t U1, uint32_t U2,
+                                             __nv_bfloat16* xrow)
+{
+    for (int j = 0; j < kFeat; j++) {
+        uint32_t ph = (uint32_t)freq[3 * j] * U0 + (uint32_t)freq[3 * j + 1] * U1 +
+                      (uint32_t)freq[3 * j + 2] * U2;
+        float s, c;
+        __sincosf(mixed::rev_to_rad(ph), &s, &c);
+        xrow[j] = __float2bfloat16(s);
+        xrow[kFeat + j] = __float2bfloat16(c);
+    }
+}
+
+__global__ void features_kernel(const uint32_t* __restrict__ U, int n, const int* __restrict__ freq,
+                                __nv_bfloat16* __restrict__ X)
+{
+    __shared__ int fs[3 * kFeat];
+    for (int k = threadIdx.x; k < 3 * kFeat; k += blockDim.x) fs[k] = freq[k];
+    __syncthreads();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    features_row(fs, U[3 * i], U[3 * i + 1], U[3 * i + 2], X + (size_t)i * kIn);
+}
+
+// ---------------------------------------------------------------- samples
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Uniform positions (32-bit fixed point per axis) and the exact FP64 mode-sum
+// field there (the plane-wave sum of fields_fp64.cuh in the same phase form).
+__global__ void samples_kernel(uint64_t seed, long long first, int n, const tp_mode* __restrict__ modes,
+                               int nmodes, double B0z, uint32_t* __restrict__ U, float* __restrict__ T)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t id = (uint64_t)(first + i);
+    uint32_t u[3];
+    for (int k = 0; k < 3; k++) u[k] = (uint32_t)(mix64(seed ^ (id * 3 + k) * 0xD1342543DE82EF95ull) >> 32);
+    double b[3] = {0, 0, 0}, e[3] = {0, 0, 0};
+    for (int m = 0; m < nmodes; m++) {
+        const tp_mode& md = modes[m];
+        uint64_t ph = (uint64_t)(int64_t)md.n[0] * ((uint64_t)u[0] << 32) +
+                      (uint64_t)(int64_t)md.n[1] * ((uint64_t)u[1] << 32) +
+                      (uint64_t)(int64_t)md.n[2] * ((uint64_t)u[2] << 32) +
+                      ((uint64_t)(uint32_t)md.pad << 32);
+        double c = cos((double)(int64_t)ph * 3.4061215800865545e-19);
+        for (int k = 0; k < 3; k++) {
+            b[k] += md.amp_b[k] * c;
+            e[k] += md.amp_e[k] * c;
+        }
+    }
+    b[2] += B0z;
+    for (int k = 0; k < 3; k++) {
+        U[3 * i + k] = u[k];
+        T[6 * i + k] = (float)b[k];
+        T[6 * i + 3 + k] = (float)e[k];
+    }
+}
+
+// ---------------------------------------------------------------- loss, biases, AdamW
+// dY = 2 (y - t_n) / (n * 6) with t_n the normalised target; BF16 dY padded to 16 columns
+__global__ void loss_kernel(const float* __restrict__ Y, const float* __restrict__ T, int n,
+                            const float* __restrict__ mean, const float* __restrict__ istd,
+                            __nv_bfloat16* __restrict__ dY, float* __restrict__ dYf,
+                            double* __restrict__ loss)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.f;
+    if (i < n) {
+        const float scale = 2.0f / ((float)n * kOut);
+        for (int c = 0; c < kOutPad; c++) {
+            float g = 0.f;
+            if (c < kOut) {
+                float r = Y[(size_t)i * kOut + c] - (T[(size_t)i * kOut + c] - mean[c]) * istd[c];
+                l += r * r;
+                g = r * scale;
+                if (dYf) dYf[(size_t)i * kOut + c] = g;
+            }
+            dY[(size_t)i * kOutPad + c] = __float2bfloat16(g);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) l += __shfl_down_sync(0xffffffffu, l, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, (double)l);
+}
+
+// db[c] += sum_rows G[row][c] (BF16 rows of width ld)
+__global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ G, int rows, int cols, int ld,
+                                 float* __restrict__ db)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    float s = 0.f;
+    for (int r = blockIdx.y; r < rows; r += gridDim.y) s += __bfloat162float(G[(size_t)r * ld + c]);
+    atomicAdd(&db[c], s);
+}
+
+__global__ void bias_grad_f32_kernel(const float* __restrict__ G, int rows, int cols,
+                                     float* __restrict__ db)
+{
+    int c = threadIdx.x;
+    if (c >= cols) return;
+    float s = 0.f;
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) s += G[(size_t)r * cols + c];
+    atomicAdd(&db[c], s);
+}
+
+struct Adam {
+    float lr, b1, b2, eps, wd, c1, c2;  // c1 = 1 / (1 - b1^t), c2 = 1 / (1 - b2^t)
+};
+
+__global__ void adamw_kernel(float* __restrict__ p, const float* __restrict__ gr, float* __restrict__ m,
+                             float* __restrict__ v, int n, Adam a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float g = gr[i];
+    float mi = a.b1 * m[i] + (1.f - a.b1) * g;
+    float vi = a.b2 * v[i] + (1.f - a.b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    float upd = (mi * a.c1) / (sqrtf(vi * a.c2) + a.eps);
+    p[i] = p[i] - a.lr * (upd + a.wd * p[i]);
+}
+
+// BF16 copies of layer weights: W [out_pad][in] and its transpose [in][out_pad]
+__global__ void to_bf16_kernel(const float* __restrict__ w, int out, int out_pad, int in,
+                               __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wt)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= out_pad * in) return;
+    int o = i / in, k = i % in;
+    __nv_bfloat16 v = __float2bfloat16(o < out ? w[(size_t)o * in + k] : 0.f);
+    wb[i] = v;
+    if (wt) wt[(size_t)k * out_pad + o] = v;
+}
+
+}  // namespace mlp
+
+// ---------------------------------------------------------------- host model
+using namespace mlp;
+
+struct MlpState {
+    bool ready = false;
+    int freq_h[kFeat * 3];
+    // parameters (FP32 master), gradients, Adam moments: one flat buffer each
+    size_t nparam = 0;
+    size_t woff[kLayers], boff[kLayers];
+    float *p = nullptr, *gr = nullptr, *m = nullptr, *v = nullptr;
+    __nv_bfloat16 *wb[kLayers] = {}, *wt[kLayers] = {};
+    int* freq = nullptr;
+    float out_mean[kOut] = {0}, out_std[kOut] = {1, 1, 1, 1, 1, 1};
+    float *d_mean = nullptr, *d_istd = nullptr;
+    long step = 0;
+    // batch workspaces
+    int cap = 0;
+    __nv_bfloat16* X = nullptr;             // [cap][128]
+    __nv_bfloat16 *Z[4] = {}, *H[4] = {};   // [cap][256]
+    __nv_bfloat16 *G0 = nullptr, *G1 = nullptr;  // [cap][256] backward scratch
+    __nv_bfloat16* dY = nullptr;            // [cap][16]
+    float* Y = nullptr;                     // [cap][6]
+    float* dYf = nullptr;                   // [cap][6]
+    double* loss = nullptr;
+};
+
+static MlpState M;
+
+static bool mlp_alloc_params()
+{
+    if (M.p) return true;
+    size_t off = 0;
+    for (int l = 0; l < kLayers; l++) {
+        M.woff[l] = off;
+        off += (size_t)layer_out(l) * layer_in(l);
+        M.boff[l] = off;
+        off += layer_out(l);
+    }
+    M.nparam = off;
+    size_t b = sizeof(float) * off;
+    if (!cuda_ok(cudaMalloc(&M.p, b), "mlp params") || !cuda_ok(cudaMalloc(&M.gr, b), "mlp grads") ||
+        !cuda_ok(cudaMalloc(&M.m, b), "mlp m") || !cuda_ok(cudaMalloc(&M.v, b), "mlp v"))
+        return false;
+    for (int l = 0; l < kLayers; l++) {
+        size_t e = (size_t)layer_out_pad(l) * layer_in(l);
+        if (!cuda_ok(cudaMalloc(&M.wb[l], sizeof(__nv_bfloat16) * e), "mlp wb") ||
+            !cuda_ok(cudaMalloc(&M.wt[l], sizeof(__nv_bfloat16) * e), "mlp wt"))
+            return false;
+    }
+    return cuda_ok(cudaMalloc(&M.freq, sizeof(int) * 3 * kFeat), "mlp freq") &&
+           cuda_ok(cudaMalloc(&M.d_mean, sizeof(float) * kOut), "mlp mean") &&
+           cuda_ok(cudaMalloc(&M.d_istd, sizeof(float) * kOut), "mlp std") &&
+           cuda_ok(cudaMalloc(&M.loss, sizeof(double)), "mlp loss");
+}
+
+static bool mlp_reserve(int n)
+{
+    if (n <= M.cap) return true;
+    auto fr = [](void* p) { if (p) cudaFree(p); };
+    fr(M.X); fr(M.G0); fr(M.G1); fr(M.dY); fr(M.Y); fr(M.dYf);
+    for (int l = 0; l < 4; l++) { fr(M.Z[l]); fr(M.H[l]); }
+    size_t h = sizeof(__nv_bfloat16) * (size_t)n * kHid;
+    bool ok = cuda_ok(cudaMalloc(&M.X, sizeof(__nv_bfloat16) * (size_t)n * kIn), "X") &&
+              cuda_ok(cudaMalloc(&M.G0, h), "G0") && cuda_ok(cudaMalloc(&M.G1, h), "G1") &&
+              cuda_ok(cudaMalloc(&M.dY, sizeof(__nv_bfloat16) * (size_t)n * kOutPad), "dY") &&
+              cuda_ok(cudaMalloc(&M.Y, sizeof(float) * (size_t)n * kOut), "Y") &&
+              cuda_ok(cudaMalloc(&M.dYf, sizeof(float) * (size_t)n * kOut), "dYf");
+    for (int l = 0; l < 4 && ok; l++)
+        ok = cuda_ok(cudaMalloc(&M.Z[l], h), "Z") && cuda_ok(cudaMalloc(&M.H[l], h), "H");
+    if (ok) M.cap = n;
+    return ok;
+}
+
+static bool mlp_refresh_bf16()
+{
+    cudaStream_t s = g.stream;
+    for (int l = 0; l < kLayers; l++) {
+        int e = layer_out_pad(l) * layer_in(l);
+        to_bf16_kernel<<<(e + 255) / 256, 256, 0, s>>>(M.p + M.woff[l], layer_out(l), layer_out_pad(l),
+                                                       layer_in(l), M.wb[l], M.wt[l]);
+    }
+    float istd[kOut];
+    for (int c = 0; c < kOut; c++) istd[c] = 1.0f / M.out_std[c];
+    cudaMemcpyAsync(M.d_mean, M.out_mean, sizeof(float) * kOut, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(M.d_istd, istd, sizeof(float) * kOut, cudaMemcpyHostToDevice, s);
+    return cuda_ok(cudaGetLastError(), "bf16 refresh");
+}
+
+// forward of n samples from features X: fills Z/H and Y (normalised outputs)
+static bool mlp_forward(int n)
+{
+    cudaStream_t s = g.stream;
+    const __nv_bfloat16* in = M.X;
+    int ldin = kIn;
+    for (int l = 0; l < 4; l++) {
+        EpiHidden e{M.p + M.boff[l], M.Z[l], M.H[l], kHid};
+        if (!cuda_ok(gemm<false, false>(in, ldin, M.wb[l], layer_in(l), n, kHid, layer_in(l), 1, e, s),
+                     "fwd gemm")) return false;
+        in = M.H[l];
+        ldin = kHid;
+    }
+    EpiOut eo{M.p + M.boff[4], M.Y, kOut};
+    return cuda_ok(gemm<false, false>(in, kHid, M.wb[4], kHid, n, kOut, kHid, 1, eo, s), "out gemm");
+}
+
+// backward of n samples after mlp_forward and the loss kernel: fills M.gr
+static bool mlp_backward(int n)
+{
+    cudaStream_t s = g.stream;
+    cudaMemsetAsync(M.gr, 0, sizeof(float) * M.nparam, s);
+    const int split = n >= 8192 ? (n + 4095) / 4096 : 1;
+    // output layer: dW4 = dYᵀ H3, db4 = sum dY, dH3 = dY W4
+    {
+        EpiAtomic ew{M.gr + M.woff[4], kHid};
+        if (!cuda_ok(gemm<true, true>(M.dY, kOutPad, M.H[3], kHid, kOut, kHid, n, split, ew, s), "dW4"))
+            return false;
+        bias_grad_f32_kernel<<<256, 32, 0, s>>>(M.dYf, n, kOut, M.gr + M.boff[4]);
+        EpiBackSilu eb{M.Z[3], M.G0, kHid};
+        if (!cuda_ok(gemm<false, false>(M.dY, kOutPad, M.wt[4], kOutPad, n, kHid, kOutPad, 1, eb, s), "dH3"))
+            return false;
+    }
+    __nv_bfloat16 *gcur = M.G0, *gnext = M.G1;
+    for (int l = 3; l >= 0; l--) {
+        const __nv_bfloat16* xin = l == 0 ? M.X : M.H[l - 1];
+        int kin = layer_in(l);
+        EpiAtomic ew{M.gr + M.woff[l], kin};
+        if (!cuda_ok(gemm<true, true>(gcur, kHid, xin, kin, kHid, kin, n, split, ew, s), "dW"))
+            return false;
+        dim3 bg((kHid + 127) / 128, 64);
+        bias_grad_kernel<<<bg, 128, 0, s>>>(gcur, n, kHid, kHid, M.gr + M.boff[l]);
+        if (l > 0) {
+            EpiBackSilu eb{M.Z[l - 1], gnext, kHid};
+            if (!cuda_ok(gemm<false, false>(gcur, kHid, M.wt[l], kHid, n, kHid, kHid, 1, eb, s), "dH"))
+                return false;
+            __nv_bfloat16* tmp = gcur;
+            gcur = gnext;
+            gnext = tmp;
+        }
+    }
+    return true;
+}
+
+static bool mlp_loss(int n, const float* T, double* loss_out)
+{
+    cudaStream_t s = g.stream;
+    cudaMemsetAsync(M.loss, 0, sizeof(double), s);
+    loss_kernel<<<(n + 255) / 256, 256, 0, s>>>(M.Y, T, n, M.d_mean, M.d_istd, M.dY, M.dYf, M.loss);
+    if (loss_out) {
+        cudaMemcpyAsync(loss_out, M.loss, sizeof(double), cudaMemcpyDeviceToHost, s);
+        if (!cuda_ok(cudaStreamSynchronize(s), "loss")) return false;
+        *loss_out /= (double)n * kOut;
+    }
+    return cuda_ok(cudaGetLastError(), "loss");
+}
+
+bool mlp_model(Model& md)
+{
+    if (!M.ready) {
+        set_error(12, "the learned field model is not trained (tp_mlp_train)");
+        return false;
+    }
+    for (int l = 0; l < kLayers; l++) {
+        md.w[l] = M.wb[l];
+        md.b[l] = M.p + M.boff[l];
+    }
+    md.freq = M.freq;
+    for (int c = 0; c < kOut; c++) {
+        md.out_scale[c] = M.out_std[c];
+        md.out_shift[c] = M.out_mean[c];
+    }
+    return true;
+}
+
+}  // namespace tp
+
+using namespace tp;
+
+// Initialise the model: frequencies (kFeat x 3 lattice vectors) and weights
+// (flat FP32 layout W0, b0, ..., W4, b4 with W_l [out][in]); NULL weights:
+// seeded He-uniform initialisation.
+extern "C" int tp_mlp_init(const int* freq, const float* weights, unsigned long long seed)
+{
+    if (!ensure_init() || !mlp_alloc_params()) return -1;
+    memcpy(M.freq_h, freq, sizeof(int) * 3 * kFeat);
+    cudaMemcpyAsync(M.freq, freq, sizeof(int) * 3 * kFeat, cudaMemcpyHostToDevice, g.stream);
+    std::vector<float> h(M.nparam, 0.f);
+    if (weights) {
+        memcpy(h.data(), weights, sizeof(float) * M.nparam);
+    } else {
+        uint64_t st = seed * 2654435761ull + 1;
+        auto rnd = [&]() {
+            st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+            return (double)(st >> 11) * (1.0 / 9007199254740992.0);
+        };
+        for (int l = 0; l < kLayers; l++) {
+            double lim = std::sqrt(6.0 / layer_in(l));
+            if (l == kLayers - 1) lim *= 0.5;
+            for (size_t k = 0; k < (size_t)layer_out(l) * layer_in(l); k++)
+                h[M.woff[l] + k] = (float)((2.0 * rnd() - 1.0) * lim);
+        }
+    }
+    cudaMemcpyAsync(M.p, h.data(), sizeof(float) * M.nparam, cudaMemcpyHostToDevice, g.stream);
+    cudaMemsetAsync(M.m, 0, sizeof(float) * M.nparam, g.stream);
+    cudaMemsetAsync(M.v, 0, sizeof(float) * M.nparam, g.stream);
+    M.step = 0;
+    M.ready = true;
+    return mlp_refresh_bf16() && cuda_ok(cudaStreamSynchronize(g.stream), "mlp init") ? 0 : -1;
+}
+
+extern "C" int tp_mlp_param_count(void)
+{
+    int n = 0;
+    for (int l = 0; l < kLayers; l++) n += layer_out(l) * layer_in(l) + layer_out(l);
+    return n;
+}
+
+extern "C" int tp_mlp_set_output_norm(const float* mean, const float* stdv)
+{
+    for (int c = 0; c < kOut; c++) {
+        M.out_mean[c] = mean[c];
+        M.out_std[c] = stdv[c];
+    }
+    return M.ready && mlp_refresh_bf16() ? 0 : -1;
+}
+
+extern "C" int tp_mlp_get_weights(float* weights)
+{
+    if (!M.ready) return -1;
+    cudaMemcpyAsync(weights, M.p, sizeof(float) * M.nparam, cudaMemcpyDeviceToHost, g.stream);
+    return cuda_ok(cudaStreamSynchronize(g.stream), "get weights") ? 0 : -1;
+}
+
+// One forward + backward on given samples (u: n*3 box fractions as 32-bit fixed
+// point, t: n*6 targets); returns the loss, the normalised outputs and the FP32
+// gradients in the flat parameter layout.  For gradient checks.
+extern "C" int tp_mlp_grad(int n, const unsigned int* u, const float* t, double* loss, float* y,
+                           float* grads)
+{
+    if (!M.ready || !mlp_reserve(n)) return -1;
+    cudaStream_t s = g.stream;
+    uint32_t* dU;
+    float* dT;
+    if (!cuda_ok(cudaMalloc(&dU, sizeof(uint32_t) * 3 * n), "u") ||
+        !cuda_ok(cudaMalloc(&dT, sizeof(float) * 6 * n), "t")) return -1;
+    cudaMemcpyAsync(dU, u, sizeof(uint32_t) * 3 * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(dT, t, sizeof(float) * 6 * n, cudaMemcpyHostToDevice, s);
+    features_kernel<<<(n + 127) / 128, 128, 0, s>>>(dU, n, M.freq, M.X);
+    bool ok = mlp_forward(n) && mlp_loss(n, dT, loss) && mlp_backward(n);
+    if (ok) {
+        if (y) cudaMemcpyAsync(y, M.Y, sizeof(float) * 6 * n, cudaMemcpyDeviceToHost, s);
+        if (grads) cudaMemcpyAsync(grads, M.gr, sizeof(float) * M.nparam, cudaMemcpyDeviceToHost, s);
+        ok = cuda_ok(cudaStreamSynchronize(s), "grad");
+    }
+    cudaFree(dU);
+    cudaFree(dT);
+    return ok ? 0 : -1;
+}
+
+// Train on nsamples field samples of the current mode table (tp_set_modes),
+// drawn uniformly in the box from `seed` and evaluated with the FP64 mode sum.
+// Output normalisation comes from the samples.  lr: peak AdamW rate with a
+// cosine decay over epochs * (nsamples / batch) steps.  Returns the final
+// mean loss (normalised units) in *loss_out and the device time in *ms_out.
+extern "C" int tp_mlp_train(long long nsamples, int batch, int epochs, double lr, double wd,
+                            unsigned long long seed, double* loss_out, double* ms_out)
+{
+    if (!M.ready) {
+        set_error(12, "tp_mlp_init first");
+        return -1;
+    }
+    if (g.modes.empty()) {
+        set_error(12, "no mode table to learn (tp_set_modes)");
+        return -1;
+    }
+    if (batch < 128 || batch % 128 || nsamples < batch) {
+        set_error(12, "batch must be a positive multiple of 128 not above nsamples");
+        return -1;
+    }
+    cudaStream_t s = g.stream;
+    DevField f;
+    if (!build_field(TP_SYS_MODESUM, f) || !mlp_reserve(batch)) return -1;
+    uint32_t* dU = nullptr;
+    float* dT = nullptr;
+    if (!cuda_ok(cudaMalloc(&dU, sizeof(uint32_t) * 3 * (size_t)nsamples), "train u") ||
+        !cuda_ok(cudaMalloc(&dT, sizeof(float) * 6 * (size_t)nsamples), "train t")) return -1;
+    for (long long off = 0; off < nsamples; off += 1 << 22) {
+        int cnt = (int)std::min<long long>(1 << 22, nsamples - off);
+        samples_kernel<<<(cnt + 127) / 128, 128, 0, s>>>(seed, off, cnt, f.modes, f.nmodes, f.B0,
+                                                         dU + 3 * off, dT + 6 * off);
+    }
+    // output normalisation from the training targets
+    {
+        std::vector<float> ht(6 * std::min<long long>(nsamples, 1 << 20));
+        cudaMemcpyAsync(ht.data(), dT, sizeof(float) * ht.size(), cudaMemcpyDeviceToHost, s);
+        if (!cuda_ok(cudaStreamSynchronize(s), "samples")) return -1;
+        size_t cnt = ht.size() / 6;
+        for (int c = 0; c < kOut; c++) {
+            double a = 0, b = 0;
+            for (size_t i = 0; i < cnt; i++) {
+                a += ht[6 * i + c];
+                b += (double)ht[6 * i + c] * ht[6 * i + c];
+            }
+            a /= cnt;
+            double var = b / cnt - a * a;
+            M.out_mean[c] = (float)a;
+            M.out_std[c] = (float)std::sqrt(var > 1e-30 ? var : 1e-30);
+        }
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    long long nb = nsamples / batch;
+    long long total = nb * epochs;
+    double loss = 0.0;
+    bool ok = mlp_refresh_bf16();
+    for (long long it = 0; it < total && ok; it++) {
+        long long bi = it % nb;
+        features_kernel<<<(batch + 127) / 128, 128, 0, s>>>(dU + 3 * bi * batch, batch, M.freq, M.X);
+        const bool last = it == total - 1;
+        ok = mlp_forward(batch) && mlp_loss(batch, dT + 6 * bi * batch, last ? &loss : nullptr) &&
+             mlp_backward(batch);
+        if (!ok) break;
+        M.step++;
+        Adam a;
+        double frac = (double)it / (double)total;
+        a.lr = (float)(lr * 0.5 * (1.0 + std::cos(M_PI * frac)));
+        a.b1 = 0.9f;
+        a.b2 = 0.999f;
+        a.eps = 1e-8f;
+        a.wd = (float)wd;
+        a.c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)M.step)));
+        a.c2 = (float)(1.0 / (1.0 - std::pow(0.999, (double)M.step)));
+        adamw_kernel<<<(int)((M.nparam + 255) / 256), 256, 0, s>>>(M.p, M.gr, M.m, M.v, (int)M.nparam, a);
+        ok = mlp_refresh_bf16();
+    }
+    cudaEventRecord(e1, s);
+    ok = ok && cuda_ok(cudaStreamSynchronize(s), "train");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(dU);
+    cudaFree(dT);
+    if (loss_out) *loss_out = loss;
+    if (ms_out) *ms_out = ms;
+    return ok ? 0 : -1;
+}
+
+// Model field at n positions (u: n*3 32-bit fixed point) through the training
+// forward pass; out: n*6 physical components.
+extern "C" int tp_mlp_eval(int n, const unsigned int* u, float* out)
+{
+    if (!M.ready || !mlp_reserve(n < 128 ? 128 : n)) return -1;
+    cudaStream_t s = g.stream;
+    uint32_t* dU;
+    if (!cuda_ok(cudaMalloc(&dU, sizeof(uint32_t) * 3 * n), "u")) return -1;
+    cudaMemcpyAsync(dU, u, sizeof(uint32_t) * 3 * n, cudaMemcpyHostToDevice, s);
+    features_kernel<<<(n + 127) / 128, 128, 0, s>>>(dU, n, M.freq, M.X);
+    bool ok = mlp_forward(n);
+    std::vector<float> y(6 * (size_t)n);
+    if (ok) {
+        cudaMemcpyAsync(y.data(), M.Y, sizeof(float) * 6 * n, cudaMemcpyDeviceToHost, s);
+        ok = cuda_ok(cudaStreamSynchronize(s), "eval");
+    }
+    cudaFree(dU);
+    if (!ok) return -1;
+    for (int i = 0; i < n; i++)
+        for (int c = 0; c < kOut; c++) out[6 * i + c] = y[6 * i + c] * M.out_std[c] + M.out_mean[c];
+    return 0;
+}

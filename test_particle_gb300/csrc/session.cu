@@ -8,6 +8,15 @@
 #include "tp_kernels.h"
 #include "tp_kernels_mixed.h"
 #include "tp_session.h"
+#include "mlp_common.cuh"
+
+namespace tp {
+namespace mlp {
+bool mlp_model(Model& md);
+cudaError_t launch_track_surrogate(const mixed::MixField& f, const Model& md, const TrackBufs& b,
+                                   const TrackParams& q, int grid, cudaStream_t s);
+}  // namespace mlp
+}  // namespace tp
 
 namespace tp {
 
@@ -81,7 +90,15 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
     mixed::MixField mf;
     int nmodes = 0;
     const bool is_mixed = rs.precision == TP_PREC_MIXED;
-    if (is_mixed) {
+    const bool is_surr = rs.precision == TP_PREC_SURROGATE;
+    mlp::Model md;
+    if (is_surr) {
+        if (system_type != TP_SYS_MODESUM) {
+            set_error(1, "the learned field model stands in for the mode-sum field (system type 5)");
+            return false;
+        }
+        if (!build_mixfield(system_type, mf, &nmodes) || !mlp::mlp_model(md)) return false;
+    } else if (is_mixed) {
         if (!build_mixfield(system_type, mf, &nmodes)) return false;
     } else if (!build_field(system_type, f)) {
         return false;
@@ -96,6 +113,7 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
     if (rs.precision == TP_PREC_FP64) bps = fp64::track_max_blocks_per_sm(system_type);
     else if (rs.precision == TP_PREC_FP64_FAST) bps = fp64fast::track_max_blocks_per_sm(system_type);
     else if (is_mixed) bps = mixed::track_max_blocks_per_sm(system_type, nmodes);
+    else if (is_surr) bps = 1;
     else {
         set_error(1, "precision %d not available for system type %d", rs.precision, system_type);
         return false;
@@ -154,6 +172,7 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
     cudaEventRecord(ev0, s);
     cudaError_t e = rs.precision == TP_PREC_FP64 ? fp64::launch_track(f, b, q, grid, s)
                   : is_mixed ? mixed::launch_track(mf, b, q, grid, s)
+                  : is_surr  ? mlp::launch_track_surrogate(mf, md, b, q, grid, s)
                              : fp64fast::launch_track(f, b, q, grid, s);
     if (!cuda_ok(e, "track launch")) return false;
     cudaEventRecord(ev1, s);

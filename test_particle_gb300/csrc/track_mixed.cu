@@ -13,122 +13,11 @@
 // rotation form: the perpendicular frame comes from h x u (no cancellation for
 // u nearly along B), 1 - cos(a) is formed as 2 sin^2(a/2), and the momentum is
 // rotated in u-space so gamma is never re-derived from |v| -> 1.
-#include "tp_mixed.cuh"
 #include "tp_kernels_mixed.h"
+#include "wirz_f32.cuh"
 
 namespace tp {
 namespace mixed {
-
-struct PM {
-    uint64_t X[3];
-    int img[3];
-    float u[3];
-};
-
-__device__ __forceinline__ float fx_to_float(uint64_t d)  // signed fixed-point delta -> box fraction
-{
-    return (float)(int64_t)d * 5.42101086242752217e-20f;  // 2^-64
-}
-
-__device__ __forceinline__ int64_t float_to_fx(float fr)  // box fraction -> signed fixed point
-{
-    return __float2ll_rn(fr * 18446744073709551616.0f);
-}
-
-// Adds a displacement (in box fractions) to a position, counting periods.
-__device__ __forceinline__ void advance(uint64_t& X, int& img, float fr)
-{
-    int64_t d = float_to_fx(fr);
-    uint64_t nx = X + (uint64_t)d;
-    if (d > 0 && nx < X) img++;
-    else if (d < 0 && nx > X) img--;
-    X = nx;
-}
-
-template <int SYS>
-__device__ __forceinline__ void wirz_mixed(const MixField& f, PM& p, float dt, const ModeF* smodes,
-                                           FieldCache& fc, bool& escaped)
-{
-    const float cm = f.cm;
-    float E[3], B[3];
-    field_mixed<SYS>(f, p.X, E, B, smodes, fc);
-    float Btot = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
-    float iB = 1.0f / Btot;
-    float h[3] = {B[0] * iB, B[1] * iB, B[2] * iB};
-    const float hk = 0.5f * cm * dt;
-    float um[3] = {p.u[0] + hk * E[0], p.u[1] + hk * E[1], p.u[2] + hk * E[2]};
-    float gam = sqrtf(1.0f + um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
-    float ig = 1.0f / gam;
-    // frame at the start point
-    float w[3] = {h[1] * um[2] - h[2] * um[1], h[2] * um[0] - h[0] * um[2], h[0] * um[1] - h[1] * um[0]};
-    float uperp = sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-    float iu = uperp > 0.0f ? 1.0f / uperp : 0.0f;
-    float hr[3] = {w[0] * iu, w[1] * iu, w[2] * iu};
-    float hp[3] = {hr[1] * h[2] - hr[2] * h[1], hr[2] * h[0] - hr[0] * h[2], hr[0] * h[1] - hr[1] * h[0]};
-    float upar = um[0] * h[0] + um[1] * h[1] + um[2] * h[2];
-    float theta = cm * Btot * ig * dt;
-    float s4, c4;
-    __sincosf(0.25f * theta, &s4, &c4);
-    float sin_h = 2.0f * s4 * c4, omc_h = 2.0f * s4 * s4;  // sin(theta/2), 1 - cos(theta/2)
-    float R = uperp / (cm * Btot);
-    float a1 = 0.5f * dt * upar * ig, a2 = R * sin_h, a3 = -R * omc_h;
-    float dpre[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) dpre[k] = (h[k] * a1 + hp[k] * a2 + hr[k] * a3) * f.invL[k];
-    uint64_t Xp[3] = {p.X[0], p.X[1], p.X[2]};
-#pragma unroll
-    for (int k = 0; k < 3; k++) Xp[k] += (uint64_t)float_to_fx(dpre[k]);
-    field_mixed<SYS>(f, Xp, E, B, smodes, fc);
-    Btot = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
-    iB = 1.0f / Btot;
-    h[0] = B[0] * iB; h[1] = B[1] * iB; h[2] = B[2] * iB;
-    w[0] = h[1] * um[2] - h[2] * um[1];
-    w[1] = h[2] * um[0] - h[0] * um[2];
-    w[2] = h[0] * um[1] - h[1] * um[0];
-    uperp = sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-    iu = uperp > 0.0f ? 1.0f / uperp : 0.0f;
-    hr[0] = w[0] * iu; hr[1] = w[1] * iu; hr[2] = w[2] * iu;
-    hp[0] = hr[1] * h[2] - hr[2] * h[1];
-    hp[1] = hr[2] * h[0] - hr[0] * h[2];
-    hp[2] = hr[0] * h[1] - hr[1] * h[0];
-    upar = um[0] * h[0] + um[1] * h[1] + um[2] * h[2];
-    theta = cm * Btot * ig * dt;
-    float s2, c2;
-    __sincosf(0.5f * theta, &s2, &c2);
-    float sn = 2.0f * s2 * c2, omc = 2.0f * s2 * s2;  // sin(theta), 1 - cos(theta)
-    float cs = 1.0f - omc;
-#pragma unroll
-    for (int k = 0; k < 3; k++) p.u[k] = h[k] * upar + uperp * (cs * hp[k] - sn * hr[k]) + hk * E[k];
-    R = uperp / (cm * Btot);
-    a1 = dt * upar * ig;
-    a2 = R * sn;
-    a3 = -R * omc;
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        float d = (h[k] * a1 + hp[k] * a2 + hr[k] * a3) * f.invL[k];
-        if (f.bc_flag == 1) {
-            // open boundary: leaving the box is an escape, not a wrap
-            int before = p.img[k];
-            advance(p.X[k], p.img[k], d);
-            if (p.img[k] != before) escaped = true;
-        } else {
-            advance(p.X[k], p.img[k], d);
-        }
-    }
-}
-
-__device__ __forceinline__ int energy_bin_f(const double* thr, int nbins, const float u[3])
-{
-    double e = (double)(sqrtf(1.0f + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) - 1.0f);
-    if (!(e < INFINITY)) return 0;
-    int lo = 0, hi = nbins - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (__ldg(thr + mid - 1) <= e) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
 
 // pitch-angle cosine of u against the local field, FP32 field, returned in double
 template <int SYS>
@@ -142,31 +31,11 @@ __device__ __forceinline__ double pitch_mu(const MixField& f, const uint64_t X[3
     return (double)((B[0] * u[0] + B[1] * u[1] + B[2] * u[2]) / (bb * uu));
 }
 
-__device__ __forceinline__ void block_diff_sum(const double sg[8], double* red, double* slot)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nwarps = blockDim.x >> 5;
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-        double v = sg[c];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-        if (lane == 0) red[warp * 8 + c] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < 8) {
-        double s = 0.0;
-        for (int w = 0; w < nwarps; w++) s += red[w * 8 + threadIdx.x];
-        slot[threadIdx.x] += s;
-    }
-    __syncthreads();
-}
-
 // Persistent fixed-step tracking in mixed precision: the same schedule and
 // diagnostics as the FP64 kernel (src/tracking.c:297-462); the mode table of
 // the plane-wave field is staged once per block in shared memory.
 template <int SYS>
-__global__ void __launch_bounds__(kBlock) track_mixed_kernel(MixField f, TrackBufs b, TrackParams q)
+__global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, TrackBufs b, TrackParams q)
 {
     __shared__ double red[(kBlock / 32) * 8];
     __shared__ unsigned int hist[kMaxSmemBins];
@@ -218,15 +87,25 @@ __global__ void __launch_bounds__(kBlock) track_mixed_kernel(MixField f, TrackBu
         if (active && esc_pre) atomicSub(&b.remain[1], 1);
         double* slot_base = b.dpart + (size_t)blockIdx.x * q.nsdc * 8;
         int done = 0;
+        // countdowns to the next diagnostic steps (j % einterval, j % 100)
+        int to_frame = q.einterval - q.sstep % q.einterval;
+        int to_diff = kDiffInterval - q.sstep % kDiffInterval;
+        if (to_frame == q.einterval) to_frame = 0;
+        if (to_diff == kDiffInterval) to_diff = 0;
         for (int j = q.sstep; j <= q.estep; j++) {
+            const bool at_diff = to_diff == 0, at_frame = to_frame == 0;
+            to_diff = at_diff ? kDiffInterval - 1 : to_diff - 1;
+            to_frame = at_frame ? q.einterval - 1 : to_frame - 1;
             sg[0] = 0.0; sg[4] = 0.0; sg[5] = 0.0;
             if (active && (esc_pre == 0 || f.bc_flag == 0)) {
                 bool e2 = false;
-                wirz_mixed<SYS>(f, p, dt, smodes, fc, e2);
+                wirz_f32(f, p, dt, [&](const uint64_t* X, float* E, float* B) {
+                    field_mixed<SYS>(f, X, E, B, smodes, fc);
+                }, e2);
                 if (e2) esc_after = 1;
                 nst += 1;
                 done += 1;
-                if (esc_after == 0 && j % kDiffInterval == 0) {
+                if (esc_after == 0 && at_diff) {
                     // calc_diff_coeff, src/diagnostics.c:659-705, FP64 accumulation
                     double t = tstart + done * q.dt;
                     double tt = t * 2 + q.dt;
@@ -253,7 +132,7 @@ __global__ void __launch_bounds__(kBlock) track_mixed_kernel(MixField f, TrackBu
             }
             if (active && esc_pre == 0 && esc_after == 1 && f.bc_flag == 1 && ntp < q.nt_out)
                 atomicAdd(&b.espect_esc[ntp * q.nbins + energy_bin_f(b.ebin_thr, q.nbins, p.u)], 1u);
-            if (j % q.einterval == 0) {
+            if (at_frame) {
                 if (ntp < q.nt_out) {
                     bool take = active && esc_after == 0;
                     if (smem_hist) {
@@ -270,11 +149,11 @@ __global__ void __launch_bounds__(kBlock) track_mixed_kernel(MixField f, TrackBu
                 }
                 ntp++;
             }
-            if (j % kDiffInterval == 0) {
+            if (at_diff) {
                 block_diff_sum(sg, red, slot_base + (size_t)tstep * 8);
                 tstep++;
             }
-            if (active && esc_after && j % kDiffInterval == 0 && tstep < q.nsdc)
+            if (active && esc_after && at_diff && tstep < q.nsdc)
                 atomicSub(&b.remain[tstep], 1);
             esc_pre = esc_after;
         }

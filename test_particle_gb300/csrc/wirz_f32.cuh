@@ -1,0 +1,151 @@
+// wirz_f32.cuh -- the FP32 Wirz push on 64-bit fixed-point positions and
+// the per-block diagnostic reductions shared by the mixed-precision kernels.
+#pragma once
+#include "tp_mixed.cuh"
+
+namespace tp {
+namespace mixed {
+
+struct PM {
+    uint64_t X[3];
+    int img[3];
+    float u[3];
+};
+
+__device__ __forceinline__ float fx_to_float(uint64_t d)  // signed fixed-point delta -> box fraction
+{
+    return (float)(int64_t)d * 5.42101086242752217e-20f;  // 2^-64
+}
+
+// Box fraction -> signed 64-bit fixed point (fr * 2^64) with 32-bit
+// conversions only (64-bit float-to-integer conversions run on the FP64 pipe,
+// a 64th of the FP32 rate on this part).  |fr| < 0.5: the integer part of
+// |fr| * 2^32 and the 32 bits below it are both exact in FP32 arithmetic.
+__device__ __forceinline__ int64_t float_to_fx(float fr)
+{
+    float a = fabsf(fr) * 4294967296.0f;
+    float fh = floorf(a);
+    uint32_t hi = __float2uint_rz(fh);
+    uint32_t lo = __float2uint_rz((a - fh) * 4294967296.0f);
+    uint64_t mag = ((uint64_t)hi << 32) | lo;
+    return fr < 0.0f ? -(int64_t)mag : (int64_t)mag;
+}
+
+// Adds a displacement (in box fractions) to a position, counting periods.
+__device__ __forceinline__ void advance(uint64_t& X, int& img, float fr)
+{
+    int64_t d = float_to_fx(fr);
+    uint64_t nx = X + (uint64_t)d;
+    if (d > 0 && nx < X) img++;
+    else if (d < 0 && nx > X) img--;
+    X = nx;
+}
+
+// One Wirz push; field(X, E, B) evaluates the field at a fixed-point position.
+template <class FieldFn>
+__device__ __forceinline__ void wirz_f32(const MixField& f, PM& p, float dt, FieldFn&& field,
+                                         bool& escaped)
+{
+    const float cm = f.cm;
+    float E[3], B[3];
+    field(p.X, E, B);
+    float Btot = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+    float iB = 1.0f / Btot;
+    float h[3] = {B[0] * iB, B[1] * iB, B[2] * iB};
+    const float hk = 0.5f * cm * dt;
+    float um[3] = {p.u[0] + hk * E[0], p.u[1] + hk * E[1], p.u[2] + hk * E[2]};
+    float gam = sqrtf(1.0f + um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
+    float ig = 1.0f / gam;
+    // frame at the start point
+    float w[3] = {h[1] * um[2] - h[2] * um[1], h[2] * um[0] - h[0] * um[2], h[0] * um[1] - h[1] * um[0]};
+    float uperp = sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    float iu = uperp > 0.0f ? 1.0f / uperp : 0.0f;
+    float hr[3] = {w[0] * iu, w[1] * iu, w[2] * iu};
+    float hp[3] = {hr[1] * h[2] - hr[2] * h[1], hr[2] * h[0] - hr[0] * h[2], hr[0] * h[1] - hr[1] * h[0]};
+    float upar = um[0] * h[0] + um[1] * h[1] + um[2] * h[2];
+    float theta = cm * Btot * ig * dt;
+    float s4, c4;
+    __sincosf(0.25f * theta, &s4, &c4);
+    float sin_h = 2.0f * s4 * c4, omc_h = 2.0f * s4 * s4;  // sin(theta/2), 1 - cos(theta/2)
+    float R = uperp / (cm * Btot);
+    float a1 = 0.5f * dt * upar * ig, a2 = R * sin_h, a3 = -R * omc_h;
+    float dpre[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) dpre[k] = (h[k] * a1 + hp[k] * a2 + hr[k] * a3) * f.invL[k];
+    uint64_t Xp[3] = {p.X[0], p.X[1], p.X[2]};
+#pragma unroll
+    for (int k = 0; k < 3; k++) Xp[k] += (uint64_t)float_to_fx(dpre[k]);
+    field(Xp, E, B);
+    Btot = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+    iB = 1.0f / Btot;
+    h[0] = B[0] * iB; h[1] = B[1] * iB; h[2] = B[2] * iB;
+    w[0] = h[1] * um[2] - h[2] * um[1];
+    w[1] = h[2] * um[0] - h[0] * um[2];
+    w[2] = h[0] * um[1] - h[1] * um[0];
+    uperp = sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    iu = uperp > 0.0f ? 1.0f / uperp : 0.0f;
+    hr[0] = w[0] * iu; hr[1] = w[1] * iu; hr[2] = w[2] * iu;
+    hp[0] = hr[1] * h[2] - hr[2] * h[1];
+    hp[1] = hr[2] * h[0] - hr[0] * h[2];
+    hp[2] = hr[0] * h[1] - hr[1] * h[0];
+    upar = um[0] * h[0] + um[1] * h[1] + um[2] * h[2];
+    theta = cm * Btot * ig * dt;
+    float s2, c2;
+    __sincosf(0.5f * theta, &s2, &c2);
+    float sn = 2.0f * s2 * c2, omc = 2.0f * s2 * s2;  // sin(theta), 1 - cos(theta)
+    float cs = 1.0f - omc;
+#pragma unroll
+    for (int k = 0; k < 3; k++) p.u[k] = h[k] * upar + uperp * (cs * hp[k] - sn * hr[k]) + hk * E[k];
+    R = uperp / (cm * Btot);
+    a1 = dt * upar * ig;
+    a2 = R * sn;
+    a3 = -R * omc;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float d = (h[k] * a1 + hp[k] * a2 + hr[k] * a3) * f.invL[k];
+        if (f.bc_flag == 1) {
+            // open boundary: leaving the box is an escape, not a wrap
+            int before = p.img[k];
+            advance(p.X[k], p.img[k], d);
+            if (p.img[k] != before) escaped = true;
+        } else {
+            advance(p.X[k], p.img[k], d);
+        }
+    }
+}
+
+__device__ __forceinline__ int energy_bin_f(const double* thr, int nbins, const float u[3])
+{
+    double e = (double)(sqrtf(1.0f + u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) - 1.0f);
+    if (!(e < INFINITY)) return 0;
+    int lo = 0, hi = nbins - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(thr + mid - 1) <= e) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void block_diff_sum(const double sg[8], double* red, double* slot)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        double v = sg[c];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) red[warp * 8 + c] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        double s = 0.0;
+        for (int w = 0; w < nwarps; w++) s += red[w * 8 + threadIdx.x];
+        slot[threadIdx.x] += s;
+    }
+    __syncthreads();
+}
+
+}  // namespace mixed
+}  // namespace tp

@@ -57,7 +57,7 @@ def test_bs_steps_vs_oracle_tight_tolerance():
         ref = po.bs_integrate(f, y0[i], 0.0, 1e-6, 60, atol=1e-10, rtol=1e-10)
         err = np.abs(rec[i] - ref) / (np.abs(ref).max(axis=0) + 1e-300)
         # libm ulps shift the controller's step sizes; orbits then separate slowly
-        assert err[:20].max() < 1e-8, (i, err[:20].max())
+        assert err[:3].max() < 1e-9, (i, err[:3].max())
         assert err.max() < 1e-4, (i, err.max())
 
 

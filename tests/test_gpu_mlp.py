@@ -1,0 +1,108 @@
+"""The learned field model: tensor-core training gradients against the FP64
+oracle, the two inference paths against each other, training against the
+mode-sum field it learns, and tracking with it against the exact field."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as mo
+
+pytestmark = pytest.mark.gpu
+tp = pytest.importorskip("test_particle_gb300")
+import test_particle_gb300.workloads as wl  # noqa: E402
+
+
+def bf16_round(a):
+    a = np.asarray(a, dtype=np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def lattice_freq(seed=3):
+    rng = np.random.default_rng(seed)
+    f = rng.integers(-8, 9, size=(64, 3))
+    f[np.all(f == 0, axis=1)] = [1, 0, 0]
+    return f
+
+
+def test_gradients_match_fp64_oracle():
+    freq = lattice_freq()
+    tp.mlp_init(freq, seed=5)
+    tp.mlp_set_output_norm(np.zeros(6), np.ones(6))
+    w = tp.mlp_weights()
+    rng = np.random.default_rng(11)
+    n = 1024
+    u = rng.integers(0, 2 ** 32, size=(n, 3), dtype=np.uint64).astype(np.uint32)
+    t = rng.normal(0, 1, size=(n, 6)).astype(np.float32)
+    loss, y, g = tp.mlp_grad(u, t)
+    # the device computes with BF16 weights and features: give the oracle the same
+    wq = w.astype(np.float64)
+    off = 0
+    for i, o in mo.SIZES:
+        wq[off:off + i * o] = bf16_round(w[off:off + i * o])
+        off += i * o + o
+    x = bf16_round(mo.features(u, freq)).astype(np.float64)
+    rloss, ry, rg = mo.loss_and_grads(wq, x, t.astype(np.float64))
+    assert abs(loss - rloss) / rloss < 2e-2
+    assert np.abs(y - ry).max() < 0.05 * np.abs(ry).max()
+    off = 0
+    for l, (i, o) in enumerate(mo.SIZES):
+        for name, sz in (("W", i * o), ("b", o)):
+            a, b = g[off:off + sz], rg[off:off + sz]
+            off += sz
+            rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+            cos = a @ b / (np.linalg.norm(a) * np.linalg.norm(b))
+            assert rel < 0.05 and cos > 0.998, (l, name, rel, cos)
+
+
+def small_modes(seed=21):
+    return wl.kolmogorov_modes(16, 1, 4, 0.5, seed, va=0.1)
+
+
+def test_training_learns_a_small_field():
+    modes = small_modes()
+    dom = tp.Domain()
+    dom.xmax = dom.ymax = dom.zmax = 1.0
+    tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=1.0)
+    # the field's own lattice vectors among the features
+    freq = np.zeros((64, 3), dtype=np.int64)
+    freq[:16] = modes["n"]
+    freq[16:] = lattice_freq(4)[16:] // 2 + np.array([1, 0, 0])
+    tp.mlp_init(freq, seed=9)
+    loss, ms = tp.mlp_train(1 << 20, 8192, 3, lr=2e-3)
+    assert loss < 1e-2, loss
+    rng = np.random.default_rng(2)
+    u = rng.integers(0, 2 ** 32, size=(4096, 3), dtype=np.uint64).astype(np.uint32)
+    xyzt = np.zeros((4096, 4))
+    xyzt[:, :3] = u / 2 ** 32
+    exact = tp.get_emf(xyzt)
+    model = tp.mlp_eval(u)
+    err_b = np.sqrt(np.mean((model[:, :3] - exact[:, :3]) ** 2)) / np.sqrt(np.mean((exact[:, :3] - [0, 0, 1]) ** 2))
+    assert err_b < 0.1, err_b
+    # the in-kernel evaluation path agrees with the training forward pass
+    mk = tp.mlp_eval_kernel(u)
+    assert np.abs(mk - model).max() < 2e-2 * np.abs(model).max()
+
+
+def test_surrogate_tracking_runs_and_tracks_the_exact_field():
+    modes = small_modes()
+    dom = tp.Domain()
+    dom.xmax = dom.ymax = dom.zmax = 1.0
+    steps = 400
+    dt = wl.gyro_dt(0.7, 1.0)
+    dom.tmax = steps * dt + 0.5 * dt
+    tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=1.0)
+    freq = np.zeros((64, 3), dtype=np.int64)
+    freq[:16] = modes["n"]
+    freq[16:] = lattice_freq(4)[16:] // 2 + np.array([1, 0, 0])
+    tp.mlp_init(freq, seed=9)
+    tp.mlp_train(1 << 20, 8192, 3, lr=2e-3)
+    tp.set_spectrum(200, 1e-3, 1e2)
+    p0 = wl.shell_particles(4096, 0.7, (0, 0, 0), (1, 1, 1), 8)
+    a = tp.track(p0, dt, 4, 200, precision=tp.PREC_MIXED)
+    b = tp.track(p0, dt, 4, 200, precision=tp.PREC_SURROGATE)
+    assert b["espect"].sum() == a["espect"].sum() == 4 * 4096
+    assert np.all(b["nsteps"] == steps + 1)
+    sa, sb = a["espect"] / 4096, b["espect"] / 4096
+    assert np.all(np.abs(sa - sb).sum(axis=1) < 0.5)
+    assert tp.device_status() == 0
