@@ -498,7 +498,7 @@ static bool mlp_loss(int n, const float* T, double* loss_out)
     return cuda_ok(cudaGetLastError(), "loss");
 }
 
-bool mlp_model(Model& md)
+bool mlp::mlp_model(Model& md)
 {
     if (!M.ready) {
         set_error(12, "the learned field model is not trained (tp_mlp_train)");

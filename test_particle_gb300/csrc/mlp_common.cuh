@@ -27,6 +27,9 @@ struct Model {
     float out_scale[kOut], out_shift[kOut];  // y = net * scale + shift
 };
 
+// Device view of the trained model (host side; false and an error if untrained).
+bool mlp_model(Model& md);
+
 __device__ __forceinline__ float silu(float z)
 {
     // z * sigmoid(z) = 0.5 z (1 + tanh(z / 2)): one MUFU op per element

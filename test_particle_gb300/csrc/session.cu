@@ -12,7 +12,6 @@
 
 namespace tp {
 namespace mlp {
-bool mlp_model(Model& md);
 cudaError_t launch_track_surrogate(const mixed::MixField& f, const Model& md, const TrackBufs& b,
                                    const TrackParams& q, int grid, cudaStream_t s);
 }  // namespace mlp

@@ -16,8 +16,6 @@
 namespace tp {
 namespace mlp {
 
-bool mlp_model(Model& md);
-
 constexpr int kB = 128;            // particles (rows) per block
 constexpr int kLD = kHid + 8;      // activation row stride (bf16), conflict-free fragments
 constexpr int kWRows = 64;         // weight rows staged per chunk
