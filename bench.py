@@ -216,6 +216,149 @@ def profile_case(prec):
     sess.close()
 
 
+def config_bench(name, args):
+    """Secondary workloads (not the headline line): pushes/s per precision and
+    the accuracy of the fast paths against the FP64 path on the same inputs."""
+    import ctypes as C
+    import test_particle_gb300 as tp
+    import test_particle_gb300.workloads as wl
+    tp.check(tp.lib().tp_init(0), "tp_init")
+    out = {"config": name}
+    if name in ("abc", "modesum", "surrogate"):
+        if name == "abc":
+            cfg = wl.config_abc()
+            dom = tp.Domain()
+            dom.xmax = dom.ymax = dom.zmax = 1.0
+            tp.configure(system_type=tp.SYS_FORCEFREE, dom=dom, abc=(1.0, 1.0, 1.0), B0=1.0,
+                         lambda0=2 * np.pi)
+        else:
+            cfg = wl.config_modesum()
+            dom = tp.Domain()
+            dom.xmax = dom.ymax = dom.zmax = 1.0
+            modes = wl.kolmogorov_modes(cfg["nmodes"], cfg["kmin"], cfg["kmax"], cfg["dB"], cfg["seed"],
+                                        va=cfg["va"])
+            tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=cfg["B0"])
+        tp.set_spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
+        dt = cfg["dt"]
+        out.update(workload=cfg["name"], dt=dt)
+        if name == "surrogate":
+            # features: the 64 strongest modes' lattice vectors
+            amp = np.linalg.norm(modes["amp_b"], axis=1)
+            freq = modes["n"][np.argsort(-amp)[:64]]
+            tp.mlp_init(freq, seed=3)
+            loss, ms = tp.mlp_train(16777216, 65536, args.epochs, lr=2e-3)
+            rng = np.random.default_rng(5)
+            u = rng.integers(0, 2 ** 32, size=(65536, 3), dtype=np.uint64).astype(np.uint32)
+            xyzt = np.zeros((len(u), 4))
+            xyzt[:, :3] = u / 2 ** 32
+            exact = tp.get_emf(xyzt)
+            model = tp.mlp_eval_kernel(u)
+            dB = exact[:, :3] - [0, 0, cfg["B0"]]
+            out["train"] = {"samples": 16777216, "epochs": args.epochs, "final_loss": loss,
+                            "train_ms": ms,
+                            "rel_rms_err_dB": float(np.sqrt(np.mean((model[:, :3] - exact[:, :3]) ** 2) /
+                                                            np.mean(dB ** 2))),
+                            "rel_rms_err_E": float(np.sqrt(np.mean((model[:, 3:] - exact[:, 3:]) ** 2) /
+                                                           np.mean(exact[:, 3:] ** 2)))}
+        n = args.nptl or cfg["nptl"]
+        steps = args.run_steps or cfg["steps"]
+        p0 = wl.shell_particles(n, cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"])
+        precs = {"abc": [("fp64", tp.PREC_FP64), ("fp64fast", tp.PREC_FP64_FAST), ("mixed", tp.PREC_MIXED)],
+                 "modesum": [("fp64", tp.PREC_FP64), ("mixed", tp.PREC_MIXED)],
+                 "surrogate": [("surrogate", tp.PREC_SURROGATE), ("mixed", tp.PREC_MIXED)]}[name]
+        sess = tp.Session(n)
+        rates = {}
+        for label, code in precs:
+            st = min(steps, args.fp64_steps_cap) if label.startswith("fp64") else steps
+            tp.set_tmax(st * dt + 0.5 * dt)
+            sess.load(p0)
+            info = sess.track(dt, max(1, st // 1000), cfg["nbins"], code)
+            rates[label] = {"pushes_per_s": info.pushes / info.kernel_ms * 1e3, "steps": st,
+                            "particles": n, "kernel_ms": info.kernel_ms}
+        out["rates"] = rates
+        # accuracy of the fast path(s) against FP64 (or against the exact field for the surrogate)
+        na, sa = args.acc_nptl, args.acc_steps
+        pa = wl.shell_particles(na, cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"] + 1)
+        pb = pa.copy()
+        rng = np.random.default_rng(77)
+        for k in ("ux", "uy", "uz"):  # 1-ulp-level perturbation: the FP64-vs-FP64 noise floor
+            pb[k] = pa[k] * (1 + 1e-15 * rng.standard_normal(na))
+        tp.set_tmax(sa * dt + 0.5 * dt)
+        ref_code = tp.PREC_MIXED if name == "surrogate" else tp.PREC_FP64
+        runs = {}
+        for label, code, pp in (("ref", ref_code, pa), ("ref_perturbed", ref_code, pb),
+                                ("fast", tp.PREC_SURROGATE if name == "surrogate" else tp.PREC_MIXED, pa)):
+            s2 = tp.Session(na)
+            s2.load(pp)
+            info = s2.track(dt, 10, cfg["nbins"], code)
+            runs[label] = s2.fetch(10, cfg["nbins"], info.nsdc)
+            s2.close()
+
+        def spec_l1(a, b):
+            return float(np.abs(a["espect"][-1] / na - b["espect"][-1] / na).sum())
+
+        def dc_rel(a, b):
+            x, y = a["dsum"][:, -1], b["dsum"][:, -1]
+            return [float(v) for v in np.abs(x - y) / np.maximum(np.abs(y), 1e-300)]
+        out["accuracy"] = {"particles": na, "steps": sa, "against": "fp64" if name != "surrogate" else "exact mode sum (mixed)",
+                           "spectrum_l1_fast": spec_l1(runs["fast"], runs["ref"]),
+                           "spectrum_l1_noise_floor": spec_l1(runs["ref_perturbed"], runs["ref"]),
+                           "diffusion_rel_err_fast": dc_rel(runs["fast"], runs["ref"]),
+                           "diffusion_rel_err_noise_floor": dc_rel(runs["ref_perturbed"], runs["ref"]),
+                           "diffusion_order": ["drr", "dxx", "dyy", "dzz", "dpp", "duu", "daa", "dee"]}
+        sess.close()
+    elif name == "bs":
+        # one circular loop (radius 1, current 1, no wire), E = 0; particles on a
+        # torus around the wire, |v| in [0.1, 0.9] c; the reference's equations
+        # (beta form, positions in L0, CGS q/m of a proton); rtol = atol = 1e-10
+        dom = tp.Domain()
+        for a in ("xmin", "ymin", "zmin"):
+            setattr(dom, a, -3.0)
+        for a in ("xmax", "ymax", "zmax"):
+            setattr(dom, a, 3.0)
+        w = tp.Wlcs()
+        w.costheta_wr = w.cosphi_wr = w.cosalpha_lp = w.cosbeta_lp = 1.0
+        w.cur_lp, w.r_lp, w.omega = 1.0, 1.0, 0.001
+        tp.configure(system_type=tp.SYS_WLCS, charge_mass=9.58e3, bc_flag=2, dom=dom, wl=[w])
+        n = args.nptl or 1048576
+        t_end = 0.05
+        tp.set_spectrum(100, 1e-3, 10.0)
+        y0 = wl.torus_particles(n, 1.0, 0.05, 0.3, 0.1, 0.9, 31)
+        L = tp.lib()
+        res = {}
+        for rep in range(2):
+            y = y0.copy()
+            t = np.zeros(n)
+            steps = np.zeros(n, dtype=np.int32)
+            st = np.zeros(n, dtype=np.int32)
+            esp = np.zeros(10 * 100)
+            dfr = np.zeros(8 * 11)
+            info = tp.RunInfo()
+            tp.check(L.tp_bs_run(C.c_int(n), tp._ptr(y), tp._ptr(t), C.c_double(t_end), C.c_int(10),
+                                 C.c_int(100), C.c_double(1e-6), C.c_double(1e-10), C.c_double(1e-10),
+                                 C.c_int(8), C.c_int(0), C.c_int(1000000), tp._ptr(steps), tp._ptr(st),
+                                 tp._ptr(esp), tp._ptr(dfr), C.byref(info)), "bs_run")
+            res = {"accepted_steps_per_s": info.pushes / info.kernel_ms * 1e3,
+                   "kernel_ms": info.kernel_ms, "particles": n, "t_end": t_end,
+                   "steps_min_median_max": [int(steps.min()), float(np.median(steps)), int(steps.max())],
+                   "status_nonzero": int((st != 0).sum()),
+                   "beta_rel_drift_max": float(np.max(np.abs(np.linalg.norm(y[:, 3:], axis=1) /
+                                                             np.linalg.norm(y0[:, 3:], axis=1) - 1)))}
+        out.update(workload="wire_loop_bs_%dptl" % n, rates={"bs_fp64": res})
+        if args.cpu_bs:
+            from oracle import pyoracle as po
+            cores = os.cpu_count() or 1
+            m = cores * 16
+            f = po.make_field(system_type=1, charge_mass=9.58e3, bc_flag=2,
+                              dom=po.Domain.from_buffer_copy(dom), wl=[po.Wlcs.from_buffer_copy(w)])
+            t0 = time.perf_counter()
+            nsteps = po.bs_run_many(f, y0[:m], 1e-6, 100, atol=1e-10, rtol=1e-10, nthreads=cores)
+            dtc = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": nsteps / dtc, "unit": "accepted steps/s", "cores": cores,
+                                   "kind": "port", "sample": "%d particles x 100 steps" % m}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -224,12 +367,24 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--config", choices=["abc", "modesum", "surrogate", "bs"], default=None,
+                    help="secondary workload instead of the headline line")
+    ap.add_argument("--nptl", type=int, default=0)
+    ap.add_argument("--run-steps", type=int, default=0)
+    ap.add_argument("--fp64-steps-cap", type=int, default=1000)
+    ap.add_argument("--acc-nptl", type=int, default=65536)
+    ap.add_argument("--acc-steps", type=int, default=2000)
+    ap.add_argument("--epochs", type=int, default=4)
+    ap.add_argument("--cpu-bs", action="store_true")
     ap.add_argument("--profile", choices=["mixed", "fp64", "fp64fast"], default=None,
                     help="one tracking launch of a small case (256^3 grid, 131072 particles, "
                          "200 steps) for a profiler capture")
     args = ap.parse_args()
     if args.profile:
         profile_case(args.profile)
+        return
+    if args.config:
+        config_bench(args.config, args)
         return
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":

@@ -108,6 +108,7 @@ def oracle():
         _oracle.or_energy_bin.restype = C.c_int
         _oracle.or_energy_bin_e.restype = C.c_int
         _oracle.or_bs_integrate.restype = C.c_int
+        _oracle.or_bs_run_many.restype = C.c_long
     return _oracle
 
 
@@ -277,3 +278,11 @@ def bs_integrate(f, y0, t0, h0, nsteps, atol=1e-5, rtol=1e-14, kmaxx=8, max_reje
     if rc != 0:
         raise ValueError("or_bs_integrate failed: %d" % rc)
     return out
+
+
+def bs_run_many(f, y0, h0, nsteps, atol=1e-10, rtol=1e-10, kmaxx=8, nthreads=0):
+    """nsteps accepted steps of every particle (OpenMP); returns the step total."""
+    cfg = OrBsCfg(atol, rtol, kmaxx, 200)
+    y = np.ascontiguousarray(y0, dtype=np.float64).copy()
+    return oracle().or_bs_run_many(C.byref(f), C.byref(cfg), C.c_int(len(y)), ptr(y), C.c_double(h0),
+                                   C.c_int(nsteps), C.c_int(nthreads))

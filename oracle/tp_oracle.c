@@ -957,3 +957,24 @@ int or_bs_integrate(const or_field *f, const or_bs_cfg *cfg, double *y, double t
     }
     return 0;
 }
+
+/* nsteps accepted steps of each of n particles (y: n*6 in/out), OpenMP over
+ * particles; returns the total accepted steps (CPU baseline driver). */
+long or_bs_run_many(const or_field *f, const or_bs_cfg *cfg, int n, double *y, double h0,
+                    int nsteps, int nthreads)
+{
+    long total = 0;
+#ifdef _OPENMP
+    int nth = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nth) reduction(+ : total)
+#endif
+    for (int i = 0; i < n; i++) {
+        double *out = (double *)malloc(sizeof(double) * 8 * (size_t)nsteps);
+        if (or_bs_integrate(f, cfg, y + 6 * (size_t)i, 0.0, h0, nsteps, out) == 0) total += nsteps;
+        free(out);
+    }
+#ifndef _OPENMP
+    (void)nthreads;
+#endif
+    return total;
+}

@@ -98,6 +98,8 @@ typedef struct or_bs_cfg {
 int or_bs_integrate(const or_field *f, const or_bs_cfg *cfg, double *y, double t0,
                     double h0, int nsteps, double *out);
 void or_bs_derivs(const or_field *f, double t, const double *y, double *dydx);
+long or_bs_run_many(const or_field *f, const or_bs_cfg *cfg, int n, double *y, double h0,
+                    int nsteps, int nthreads);
 
 #ifdef __cplusplus
 }
