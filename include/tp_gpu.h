@@ -271,6 +271,52 @@ int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,
                   double *espect, double *espect_escape, double *dsum, int *remain,
                   tp_run_info *info);
 
+/* ---- Part 3: tracking without device allocation --------------------------
+ * No counterpart in the reference.  For callers that may not allocate device
+ * memory (a host framework whose allocator owns the GPU, a stream being
+ * captured into a graph, a real-time host): the caller passes every input and
+ * output as device memory; the library uses only a 4 MiB file-scope device
+ * array for its scratch and calls no allocating routine.  The first call on
+ * each device looks up that array's address (make it before any stream
+ * capture).  Calls that overlap on the GPU race on the shared scratch:
+ * serialise them.  Runs the mixed-precision tracking kernel (TP_PREC_MIXED)
+ * over steps 1..estep, system type 2 (ABC field from abc, B0, lambda0) or 4
+ * (node-interleaved grid).  The return value is 0 on success, else one of
+ * TP_NOALLOC_*; it does not wait for the kernels. */
+enum {
+    TP_NOALLOC_EINVAL = 1,   /* bad argument (pointer, size, range)           */
+    TP_NOALLOC_ETOOBIG = 2,  /* estep / 100 + 1 partial-sum rows do not fit   */
+    TP_NOALLOC_ECUDA = 3     /* a CUDA call failed                             */
+};
+
+typedef struct tp_noalloc_args {
+    int n;                 /* particles, >= 1                                  */
+    int system_type;       /* TP_SYS_FORCEFREE or TP_SYS_PIC                   */
+    int estep;             /* last step (steps 1..estep)                       */
+    int nt_out;            /* diagnostic frames; einterval = estep / nt_out    */
+    int nbins;             /* energy bins, 3..4096                             */
+    int bc_flag;           /* 0 periodic, 1 open                               */
+    int interp_corrected;  /* 0: the reference's trilinear weights             */
+    int nx, ny, nz;        /* grid nodes (system 4), >= 2 each                 */
+    double dt, charge_mass, emin, emax;
+    double lo[3], hi[3];   /* box (xmin, ymin, zmin), (xmax, ymax, zmax)       */
+    double abc[3], B0, lambda0;  /* ABC field (system 2)                       */
+    const float *d_grid;   /* system 4: per node {Ex,Ey,Ez,0,Bx,By,Bz,0},
+                              x fastest, 16-byte aligned                       */
+    double *d_state;       /* in/out, 11 * n: the particles fields as columns
+                              (x, y, z, qm, ux, uy, uz, t, xs, ys, zs)        */
+    const double *d_state0;  /* 11 * n: the initial particles, same columns   */
+    int *d_nsteps;         /* out, n: steps taken                              */
+    unsigned int *d_espect;         /* out, nt_out * nbins counts              */
+    unsigned int *d_espect_escape;  /* out, nt_out * nbins counts              */
+    double *d_dsum;        /* out, 8 rows (drr, dxx, dyy, dzz, dpp, duu, daa,
+                              dee) of estep / 100 + 1 diffusion sums          */
+    int *d_remain;         /* out, estep / 100 + 1 particles remaining         */
+    void *stream;          /* cudaStream_t, or NULL for the default stream    */
+} tp_noalloc_args;
+
+int tp_track_mixed_noalloc(const tp_noalloc_args *args);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,6 +32,7 @@ UNITS = [
     ("mlp.o", "mlp.cu", []),
     ("track_surrogate.o", "track_surrogate.cu", ["-fmad=true"]),
     ("host_config.o", "host_config.cpp", ["-x", "cu"]),
+    ("noalloc.o", "noalloc.cu", []),
 ]
 
 
