@@ -31,6 +31,12 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-pushes/s on 1 GB300: FP64 vs mixed+surrogate at stated spectrum error"
 UNIT = "pushes/s"
+# DRAM bytes (read + write) per push of track_mixed_kernel<4>, from one ncu
+# capture of `python bench.py --profile mixed` (256^3 grid, 131072 particles,
+# 200 steps: 2.163 GB for 26,214,400 pushes); the headline workload has the
+# same particle density per cell, so its traffic scales with the pushes.
+# Summary: profiles/track_mixed_kernel_pic_256cube_131072ptl.txt
+DRAM_BYTES_PER_PUSH = (2.142714e9 + 20.100864e6) / 26214400.0
 
 
 def peaks():
@@ -478,7 +484,9 @@ def main():
             "gpu_launches": launches,
             "clocks": clocks,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+                         "frac": achieved / hbm, "peak_kind": peak_kind,
+                         "traffic": DRAM_BYTES_PER_PUSH * pushes,
+                         "traffic_note": "ncu DRAM bytes of the 256^3 case scaled by pushes per launch",
                          "kernel": "track_mixed_kernel<PIC>",
                          "algorithmic_bytes_per_push": 384},
             "fp64": {"value": fp64_value * world, "unit": UNIT,

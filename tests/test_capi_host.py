@@ -136,3 +136,33 @@ def test_no_gpu_is_an_error_not_a_fallback(lib):
         pytest.skip("a GPU is present")
     with pytest.raises(RuntimeError, match="no CUDA device"):
         tp.get_emf(np.zeros((1, 4)))
+
+
+@pytest.mark.parametrize("case", ["no_step_label", "no_ff_label", "no_file", "no_wlcs_config"])
+def test_config_errors_exit_like_the_reference(tmp_path, case):
+    """Malformed or missing configuration: a message on stdout and exit(1), as
+    the reference's readers do (src/tracking.c:1226-1255, src/force_free.c:99-125);
+    adjust_dt_normI without a wire-loop configuration exits instead of
+    dereferencing NULL (src/wlcs.c:266-269).  Run in a child process."""
+    import subprocess
+    import sys
+    init = tmp_path / "init.dat"
+    init.write_text(
+        "------------------------------ Force-free field ------------------------------\n"
+        "Normalized B(Gauss): 2.5\n"
+        "------------------------------ Particle tracking -----------------------------\n"
+        "Tracking method to use: 0\n")
+    call = {
+        "no_step_label": "L.get_tracking_time_interval(0, %r, C.c_double(1.0))" % str(init).encode(),
+        "no_ff_label": "L.get_param_ff(0, %r)" % str(init).encode(),
+        "no_file": "L.get_param_ff(0, %r)" % str(tmp_path / "missing.dat").encode(),
+        "no_wlcs_config": "L.free_config(); d = C.c_double(1.0); L.adjust_dt_normI(C.byref(d))",
+    }[case]
+    code = ("import ctypes as C, test_particle_gb300 as tp\n"
+            "L = tp.lib()\nL.get_tracking_time_interval.restype = C.c_double\n" + call + "\n"
+            "print('RETURNED')\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120,
+                       cwd=ROOT)
+    assert r.returncode == 1, (r.returncode, r.stdout, r.stderr)
+    assert "RETURNED" not in r.stdout
+    assert r.stdout.strip(), "no message"
