@@ -22,7 +22,7 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcom
 UNITS = [
     ("track_fp64.o", "track_fp64.cu", ["-fmad=false"]),
     ("track_fp64fast.o", "track_fp64.cu", ["-fmad=true", "-DTP_FP64_NS=fp64fast"]),
-    ("track_mixed.o", "track_mixed.cu", ["-fmad=true"]),
+    ("track_mixed.o", "track_mixed.cu", ["-fmad=true", "-ftz=true"]),
     ("mixed_host.o", "mixed_host.cu", []),
     ("capi.o", "capi.cu", []),
     ("session.o", "session.cu", []),
@@ -30,7 +30,7 @@ UNITS = [
     ("bs.o", "bs.cu", []),
     ("synth.o", "synth.cu", []),
     ("mlp.o", "mlp.cu", []),
-    ("track_surrogate.o", "track_surrogate.cu", ["-fmad=true"]),
+    ("track_surrogate.o", "track_surrogate.cu", ["-fmad=true", "-ftz=true"]),
     ("host_config.o", "host_config.cpp", ["-x", "cu"]),
     ("noalloc.o", "noalloc.cu", []),
 ]

@@ -78,6 +78,10 @@ bool build_mixfield(int stype, mixed::MixField& mf, int* nmodes_out)
             }
             mf.interp_ref = !g.interp_corrected;
             size_t n = (size_t)mf.nx * mf.ny * mf.nz;
+            if (n >= 0xffffffffull) {
+                set_error(10, "the mixed-precision path indexes grids of fewer than 2^32 - 1 nodes");
+                return false;
+            }
             float4* v4 = (float4*)g.s_mix_v.get(sizeof(float4) * n);
             if (!v4) return false;
             interleave_v_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(f.vc_d, n, v4);
@@ -99,6 +103,10 @@ bool build_mixfield(int stype, mixed::MixField& mf, int* nmodes_out)
                 return false;
             }
         size_t n = (size_t)mf.nx * mf.ny * mf.nz;
+        if (n >= 0xffffffffull) {
+            set_error(10, "the mixed-precision path indexes grids of fewer than 2^32 - 1 nodes");
+            return false;
+        }
         if (g.eb_src_e != f.ec_f || g.eb_src_b != f.bc_f || g.eb_n != n || g.eb_gen != g.upload_gen) {
             float4* eb = (float4*)g.s_mix_eb.get(sizeof(float4) * 2 * n);
             if (!eb) return false;

@@ -125,7 +125,8 @@ extern "C" int tp_track_mixed_noalloc(const tp_noalloc_args* a)
     const int einterval = a->estep / a->nt_out;
     if (einterval < 1) return TP_NOALLOC_EINVAL;
     if (a->system_type != TP_SYS_FORCEFREE && a->system_type != TP_SYS_PIC) return TP_NOALLOC_EINVAL;
-    if (a->system_type == TP_SYS_PIC && (!a->d_grid || a->nx < 2 || a->ny < 2 || a->nz < 2))
+    if (a->system_type == TP_SYS_PIC && (!a->d_grid || a->nx < 2 || a->ny < 2 || a->nz < 2 ||
+                                         (unsigned long long)a->nx * a->ny * a->nz >= 0xffffffffull))
         return TP_NOALLOC_EINVAL;
     cudaStream_t s = static_cast<cudaStream_t>(a->stream);
 

@@ -50,17 +50,12 @@ __device__ __forceinline__ void cell_of(uint64_t X, int n, int& i, float& fr)
     fr = (float)(uint32_t)G * 2.3283064365386963e-10f;  // 2^-32
 }
 
-__device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t)
-{
-    return make_float4(fmaf(t, b.x - a.x, a.x), fmaf(t, b.y - a.y, a.y), fmaf(t, b.z - a.z, a.z), 0.f);
-}
-
 // The eight corner nodes of the cell a particle last sampled, kept in
 // registers: at a few tenths of a cell per step most evaluations fall in the
 // same cell as the previous one and need no memory traffic at all.
 template <int STRIDE>
 struct CellCache {
-    long long key = -1;
+    uint32_t key = 0xffffffffu;  // node index of the cached cell (grids hold < 2^32 - 1 nodes)
     float4 c[8 * STRIDE];
 };
 
@@ -80,10 +75,10 @@ __device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __r
         fx = fz;
         fz = t;
     }
-    const long long nx = f.nx, nxy = (long long)f.nx * f.ny;
-    const long long base = ix + nx * iy + nxy * iz;
+    const uint32_t nx = f.nx, nxy = (uint32_t)f.nx * f.ny;
+    const uint32_t base = ix + nx * iy + nxy * iz;
     if (base != cc.key) {
-        const float4* p = g + base * STRIDE;
+        const float4* p = g + (size_t)base * STRIDE;
 #pragma unroll
         for (int c = 0; c < STRIDE; c++) {
             cc.c[0 * STRIDE + c] = __ldg(p + c);
@@ -97,13 +92,21 @@ __device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __r
         }
         cc.key = base;
     }
+    // eight corner weights once, then one multiply and seven FMAs per component
+    const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
+    const float a00 = gy * gz, a10 = fy * gz, a01 = gy * fz, a11 = fy * fz;
+    const float w[8] = {gx * a00, fx * a00, gx * a10, fx * a10, gx * a01, fx * a01, gx * a11, fx * a11};
 #pragma unroll
     for (int c = 0; c < STRIDE; c++) {
-        float4 a = lerp4(cc.c[0 * STRIDE + c], cc.c[1 * STRIDE + c], fx);
-        float4 b = lerp4(cc.c[2 * STRIDE + c], cc.c[3 * STRIDE + c], fx);
-        float4 d = lerp4(cc.c[4 * STRIDE + c], cc.c[5 * STRIDE + c], fx);
-        float4 e = lerp4(cc.c[6 * STRIDE + c], cc.c[7 * STRIDE + c], fx);
-        out[c] = lerp4(lerp4(a, b, fy), lerp4(d, e, fy), fz);
+        float4 r = make_float4(w[0] * cc.c[c].x, w[0] * cc.c[c].y, w[0] * cc.c[c].z, 0.f);
+#pragma unroll
+        for (int k = 1; k < 8; k++) {
+            const float4 v = cc.c[k * STRIDE + c];
+            r.x = fmaf(w[k], v.x, r.x);
+            r.y = fmaf(w[k], v.y, r.y);
+            r.z = fmaf(w[k], v.z, r.z);
+        }
+        out[c] = r;
     }
 }
 

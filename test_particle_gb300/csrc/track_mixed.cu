@@ -34,32 +34,44 @@ __device__ __forceinline__ double pitch_mu(const MixField& f, const uint64_t X[3
 // Persistent fixed-step tracking in mixed precision: the same schedule and
 // diagnostics as the FP64 kernel (src/tracking.c:297-462); the mode table of
 // the plane-wave field is staged once per block in shared memory.
+// Per-particle data that only the diffusion steps (every 100 steps) touch --
+// the initial state, its pitch cosine, the start time and the last diffusion
+// singles -- lives in shared memory, [row][thread], so the step loop keeps
+// only the push state and the cell cache in registers.
+enum : int { DG_SG = 0, DG_X0 = 8, DG_U0 = 11, DG_T0 = 14, DG_MU0 = 15, DG_ROWS = 16 };
+
+// Persistent fixed-step tracking in mixed precision: the same schedule and
+// diagnostics as the FP64 kernel (src/tracking.c:297-462); the mode table of
+// the plane-wave field is staged once per block in shared memory.
 template <int SYS>
 __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, TrackBufs b, TrackParams q)
 {
     __shared__ double red[(kBlock / 32) * 8];
     __shared__ unsigned int hist[kMaxSmemBins];
+    __shared__ double dg[DG_ROWS][kBlock];
     extern __shared__ ModeF smodes[];
     if (SYS == TP_SYS_MODESUM) {
         for (int m = threadIdx.x; m < f.nmodes; m += blockDim.x) smodes[m] = f.modes[m];
         __syncthreads();
     }
+    const int tx = threadIdx.x;
     const bool smem_hist = q.nbins <= kMaxSmemBins;
     const float dt = (float)q.dt;
     for (int tile = blockIdx.x; tile < q.ntiles; tile += gridDim.x) {
-        const int i = tile * kBlock + threadIdx.x;
+        const int i = tile * kBlock + tx;
         const bool active = i < q.n;
         PM p = {};
         FieldCache fc;
-        double x0[3] = {0, 0, 0}, u0[3] = {0, 0, 0}, tstart = 0.0, mu0 = 0.0;
         int nst = 1;
         bool esc = false;
+#pragma unroll
+        for (int r = 0; r < DG_ROWS; r++) dg[r][tx] = 0.0;
         if (active) {
             double xs[3] = {b.x[i], b.y[i], b.z[i]};
             double sh[3] = {b.xs[i], b.ys[i], b.zs[i]};
-            x0[0] = b.x0[i]; x0[1] = b.y0[i]; x0[2] = b.z0[i];
-            u0[0] = b.ux0[i]; u0[1] = b.uy0[i]; u0[2] = b.uz0[i];
-            tstart = b.t[i];
+            double x0[3] = {b.x0[i], b.y0[i], b.z0[i]};
+            double u0[3] = {b.ux0[i], b.uy0[i], b.uz0[i]};
+            dg[DG_T0][tx] = b.t[i];
             nst = b.nsteps_ptl[i];
 #pragma unroll
             for (int k = 0; k < 3; k++) {
@@ -68,6 +80,8 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
                 if (f.bc_flag == 1 && (r < 0.0 || r > 1.0)) esc = true;
                 p.X[k] = __double2ull_rz((r - fl) * 18446744073709551616.0);
                 p.img[k] = (int)fl + (int)llrint(sh[k] / f.L[k]);
+                dg[DG_X0 + k][tx] = x0[k];
+                dg[DG_U0 + k][tx] = u0[k];
             }
             p.u[0] = (float)b.ux[i]; p.u[1] = (float)b.uy[i]; p.u[2] = (float)b.uz[i];
             // mu of the initial state: the field at the initial position is static
@@ -78,12 +92,11 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
                 double r = (x0[k] - f.min[k]) / f.L[k];
                 X0[k] = __double2ull_rz((r - floor(r)) * 18446744073709551616.0);
             }
-            mu0 = pitch_mu<SYS>(f, X0, uf0, smodes, fc);
+            dg[DG_MU0][tx] = pitch_mu<SYS>(f, X0, uf0, smodes, fc);
         }
         int esc_pre = esc ? 1 : 0;
         int esc_after = esc_pre;
         int ntp = q.ntp0, tstep = 1;
-        double sg[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         if (active && esc_pre) atomicSub(&b.remain[1], 1);
         double* slot_base = b.dpart + (size_t)blockIdx.x * q.nsdc * 8;
         int done = 0;
@@ -96,7 +109,6 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
             const bool at_diff = to_diff == 0, at_frame = to_frame == 0;
             to_diff = at_diff ? kDiffInterval - 1 : to_diff - 1;
             to_frame = at_frame ? q.einterval - 1 : to_frame - 1;
-            sg[0] = 0.0; sg[4] = 0.0; sg[5] = 0.0;
             if (active && (esc_pre == 0 || f.bc_flag == 0)) {
                 bool e2 = false;
                 wirz_f32(f, p, dt, [&](const uint64_t* X, float* E, float* B) {
@@ -107,27 +119,29 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
                 done += 1;
                 if (esc_after == 0 && at_diff) {
                     // calc_diff_coeff, src/diagnostics.c:659-705, FP64 accumulation
-                    double t = tstart + done * q.dt;
+                    double t = dg[DG_T0][tx] + done * q.dt;
                     double tt = t * 2 + q.dt;
                     double dd[3];
 #pragma unroll
                     for (int k = 0; k < 3; k++) {
                         double pos = (double)p.X[k] * 5.421010862427522e-20 + p.img[k];
-                        dd[k] = x0[k] - (f.min[k] + f.L[k] * pos);
+                        dd[k] = dg[DG_X0 + k][tx] - (f.min[k] + f.L[k] * pos);
                     }
+                    const double u00 = dg[DG_U0][tx], u01 = dg[DG_U0 + 1][tx], u02 = dg[DG_U0 + 2][tx];
+                    const double mu0 = dg[DG_MU0][tx];
                     double dxx = dd[0] * dd[0] / tt, dyy = dd[1] * dd[1] / tt, dzz = dd[2] * dd[2] / tt;
-                    double du0 = u0[0] - p.u[0], du1 = u0[1] - p.u[1], du2 = u0[2] - p.u[2];
+                    double du0 = u00 - p.u[0], du1 = u01 - p.u[1], du2 = u02 - p.u[2];
                     double g1 = sqrt(1.0 + (double)p.u[0] * p.u[0] + (double)p.u[1] * p.u[1] + (double)p.u[2] * p.u[2]);
-                    double g0 = sqrt(1.0 + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
+                    double g0 = sqrt(1.0 + u00 * u00 + u01 * u01 + u02 * u02);
                     double mu = pitch_mu<SYS>(f, p.X, p.u, smodes, fc);
                     double th = (double)acosf((float)mu) * (180.0 / 3.14159265358979323846);
                     double th0 = (double)acosf((float)mu0) * (180.0 / 3.14159265358979323846);
-                    sg[1] = dxx; sg[2] = dyy; sg[3] = dzz;
-                    sg[0] = dxx + dyy + dzz;
-                    sg[4] = (du0 * du0 + du1 * du1 + du2 * du2) / tt;
-                    sg[5] = (mu - mu0) * (mu - mu0) / tt;
-                    sg[6] = (th - th0) * (th - th0) / tt;
-                    sg[7] = (g1 - g0) * (g1 - g0) / tt;
+                    dg[DG_SG + 1][tx] = dxx; dg[DG_SG + 2][tx] = dyy; dg[DG_SG + 3][tx] = dzz;
+                    dg[DG_SG + 0][tx] = dxx + dyy + dzz;
+                    dg[DG_SG + 4][tx] = (du0 * du0 + du1 * du1 + du2 * du2) / tt;
+                    dg[DG_SG + 5][tx] = (mu - mu0) * (mu - mu0) / tt;
+                    dg[DG_SG + 6][tx] = (th - th0) * (th - th0) / tt;
+                    dg[DG_SG + 7][tx] = (g1 - g0) * (g1 - g0) / tt;
                 }
             }
             if (active && esc_pre == 0 && esc_after == 1 && f.bc_flag == 1 && ntp < q.nt_out)
@@ -137,11 +151,11 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
                     bool take = active && esc_after == 0;
                     if (smem_hist) {
                         __syncthreads();
-                        for (int k = threadIdx.x; k < q.nbins; k += blockDim.x) hist[k] = 0u;
+                        for (int k = tx; k < q.nbins; k += blockDim.x) hist[k] = 0u;
                         __syncthreads();
                         if (take) atomicAdd(&hist[energy_bin_f(b.ebin_thr, q.nbins, p.u)], 1u);
                         __syncthreads();
-                        for (int k = threadIdx.x; k < q.nbins; k += blockDim.x)
+                        for (int k = tx; k < q.nbins; k += blockDim.x)
                             if (hist[k]) atomicAdd(&b.espect[ntp * q.nbins + k], hist[k]);
                     } else if (take) {
                         atomicAdd(&b.espect[ntp * q.nbins + energy_bin_f(b.ebin_thr, q.nbins, p.u)], 1u);
@@ -150,6 +164,15 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
                 ntp++;
             }
             if (at_diff) {
+                // drr, dpp and duu are the only singles the reference clears
+                // every step (src/tracking.c:334-336); the others keep their
+                // last values for particles that no longer move
+                if (!(active && (esc_pre == 0 || f.bc_flag == 0) && esc_after == 0)) {
+                    dg[DG_SG + 0][tx] = 0.0; dg[DG_SG + 4][tx] = 0.0; dg[DG_SG + 5][tx] = 0.0;
+                }
+                double sg[8];
+#pragma unroll
+                for (int c = 0; c < 8; c++) sg[c] = dg[DG_SG + c][tx];
                 block_diff_sum(sg, red, slot_base + (size_t)tstep * 8);
                 tstep++;
             }
@@ -164,7 +187,7 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
             b.x[i] = xs[0]; b.y[i] = xs[1]; b.z[i] = xs[2];
             b.xs[i] = p.img[0] * f.L[0]; b.ys[i] = p.img[1] * f.L[1]; b.zs[i] = p.img[2] * f.L[2];
             b.ux[i] = p.u[0]; b.uy[i] = p.u[1]; b.uz[i] = p.u[2];
-            b.t[i] = tstart + done * q.dt;
+            b.t[i] = dg[DG_T0][tx] + done * q.dt;
             b.nsteps_ptl[i] = nst;
         }
     }

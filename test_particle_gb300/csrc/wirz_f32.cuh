@@ -46,20 +46,24 @@ template <class FieldFn>
 __device__ __forceinline__ void wirz_f32(const MixField& f, PM& p, float dt, FieldFn&& field,
                                          bool& escaped)
 {
-    const float cm = f.cm;
+    // Norms and their inverses come from one rsqrt each (a single SFU
+    // operation, a few ulp): the FP32 path's error budget is set by FP32
+    // rounding of the push, not by these.
+    const float cm = f.cm, icm = 1.0f / f.cm;
     float E[3], B[3];
     field(p.X, E, B);
-    float Btot = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
-    float iB = 1.0f / Btot;
+    float B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+    float iB = rsqrtf(B2);
+    float Btot = B2 * iB;
     float h[3] = {B[0] * iB, B[1] * iB, B[2] * iB};
     const float hk = 0.5f * cm * dt;
     float um[3] = {p.u[0] + hk * E[0], p.u[1] + hk * E[1], p.u[2] + hk * E[2]};
-    float gam = sqrtf(1.0f + um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
-    float ig = 1.0f / gam;
+    float ig = rsqrtf(1.0f + um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);  // 1 / gamma
     // frame at the start point
     float w[3] = {h[1] * um[2] - h[2] * um[1], h[2] * um[0] - h[0] * um[2], h[0] * um[1] - h[1] * um[0]};
-    float uperp = sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-    float iu = uperp > 0.0f ? 1.0f / uperp : 0.0f;
+    float w2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+    float iu = w2 > 0.0f ? rsqrtf(w2) : 0.0f;
+    float uperp = w2 * iu;
     float hr[3] = {w[0] * iu, w[1] * iu, w[2] * iu};
     float hp[3] = {hr[1] * h[2] - hr[2] * h[1], hr[2] * h[0] - hr[0] * h[2], hr[0] * h[1] - hr[1] * h[0]};
     float upar = um[0] * h[0] + um[1] * h[1] + um[2] * h[2];
@@ -67,7 +71,7 @@ __device__ __forceinline__ void wirz_f32(const MixField& f, PM& p, float dt, Fie
     float s4, c4;
     __sincosf(0.25f * theta, &s4, &c4);
     float sin_h = 2.0f * s4 * c4, omc_h = 2.0f * s4 * s4;  // sin(theta/2), 1 - cos(theta/2)
-    float R = uperp / (cm * Btot);
+    float R = uperp * iB * icm;  // uperp / (cm |B|)
     float a1 = 0.5f * dt * upar * ig, a2 = R * sin_h, a3 = -R * omc_h;
     float dpre[3];
 #pragma unroll
@@ -76,14 +80,16 @@ __device__ __forceinline__ void wirz_f32(const MixField& f, PM& p, float dt, Fie
 #pragma unroll
     for (int k = 0; k < 3; k++) Xp[k] += (uint64_t)float_to_fx(dpre[k]);
     field(Xp, E, B);
-    Btot = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
-    iB = 1.0f / Btot;
+    B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+    iB = rsqrtf(B2);
+    Btot = B2 * iB;
     h[0] = B[0] * iB; h[1] = B[1] * iB; h[2] = B[2] * iB;
     w[0] = h[1] * um[2] - h[2] * um[1];
     w[1] = h[2] * um[0] - h[0] * um[2];
     w[2] = h[0] * um[1] - h[1] * um[0];
-    uperp = sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-    iu = uperp > 0.0f ? 1.0f / uperp : 0.0f;
+    w2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+    iu = w2 > 0.0f ? rsqrtf(w2) : 0.0f;
+    uperp = w2 * iu;
     hr[0] = w[0] * iu; hr[1] = w[1] * iu; hr[2] = w[2] * iu;
     hp[0] = hr[1] * h[2] - hr[2] * h[1];
     hp[1] = hr[2] * h[0] - hr[0] * h[2];
@@ -96,7 +102,7 @@ __device__ __forceinline__ void wirz_f32(const MixField& f, PM& p, float dt, Fie
     float cs = 1.0f - omc;
 #pragma unroll
     for (int k = 0; k < 3; k++) p.u[k] = h[k] * upar + uperp * (cs * hp[k] - sn * hr[k]) + hk * E[k];
-    R = uperp / (cm * Btot);
+    R = uperp * iB * icm;
     a1 = dt * upar * ig;
     a2 = R * sn;
     a3 = -R * omc;
