@@ -204,14 +204,33 @@ def reference_arm(args, world, rank):
 
 
 def profile_case(prec):
-    """Small case of the headline kernel: 256^3 grid (0.5 GB interleaved,
-    larger than L2), 131072 particles, 200 steps, one launch after a warm-up."""
+    """Small case of a tracking kernel, one launch after a warm-up: the
+    gridded field (256^3, 0.5 GB interleaved, larger than L2; 131072
+    particles, 200 steps) for mixed / fp64 / fp64fast; the 512-mode field
+    with an untrained learned model (the kernel's work does not depend on the
+    weights; 155648 particles = 2 x 304 blocks of 256, 20 steps) for surrogate."""
     import test_particle_gb300 as tp
     import test_particle_gb300.workloads as wl
-    cfg = wl.config_grid(nptl=131072, steps=200, n=256)
-    dom, grd, p0, _, _ = setup_grid(tp, wl, cfg, 0)
+    if prec == "surrogate":
+        tp.check(tp.lib().tp_init(0), "tp_init")
+        cfg = wl.config_modesum(nptl=155648, steps=20)
+        dom = tp.Domain()
+        dom.xmax = dom.ymax = dom.zmax = 1.0
+        dom.tmax = cfg["steps"] * cfg["dt"] + 0.5 * cfg["dt"]
+        modes = wl.kolmogorov_modes(cfg["nmodes"], cfg["kmin"], cfg["kmax"], cfg["dB"], cfg["seed"],
+                                    va=cfg["va"])
+        tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=cfg["B0"])
+        tp.set_spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
+        amp = np.linalg.norm(modes["amp_b"], axis=1)
+        tp.mlp_init(modes["n"][np.argsort(-amp)[:64]], seed=3)
+        tp.mlp_set_output_norm(np.array([0, 0, 1, 0, 0, 0]), np.ones(6))
+        p0 = wl.shell_particles(cfg["nptl"], cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"])
+    else:
+        cfg = wl.config_grid(nptl=131072, steps=200, n=256)
+        dom, grd, p0, _, _ = setup_grid(tp, wl, cfg, 0)
     sess = tp.Session(cfg["nptl"])
-    code = {"mixed": tp.PREC_MIXED, "fp64": tp.PREC_FP64, "fp64fast": tp.PREC_FP64_FAST}[prec]
+    code = {"mixed": tp.PREC_MIXED, "fp64": tp.PREC_FP64, "fp64fast": tp.PREC_FP64_FAST,
+            "surrogate": tp.PREC_SURROGATE}[prec]
     sess.load(p0)
     sess.track(cfg["dt"], 2, cfg["nbins"], code)
     sess.load(p0)
@@ -382,9 +401,10 @@ def main():
     ap.add_argument("--acc-steps", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=4)
     ap.add_argument("--cpu-bs", action="store_true")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "fp64fast"], default=None,
-                    help="one tracking launch of a small case (256^3 grid, 131072 particles, "
-                         "200 steps) for a profiler capture")
+    ap.add_argument("--profile", choices=["mixed", "fp64", "fp64fast", "surrogate"], default=None,
+                    help="one tracking launch of a small case for a profiler capture (gridded "
+                         "field 256^3, 131072 particles, 200 steps; surrogate: 512-mode field, "
+                         "155648 particles, 20 steps)")
     args = ap.parse_args()
     if args.profile:
         profile_case(args.profile)

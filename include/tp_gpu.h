@@ -265,6 +265,12 @@ int tp_mlp_eval(int n, const unsigned int *u, float *out6);
 /* Same, through the block-wide evaluation the tracking kernel uses. */
 int tp_mlp_eval_kernel(int n, const unsigned int *u, float *out6);
 
+/* One 128-row tile of D = A * B^T on the tensor cores (tcgen05.mma, BF16
+ * operands given as raw 16-bit patterns, FP32 result): A[128][k], B[n][k],
+ * D[128][n]; n a multiple of 16 in [16, 256], k a multiple of 64 in
+ * [64, 256].  A self-check of the tensor-core path of the learned field model. */
+int tp_tc_gemm_bf16(int n, int k, const unsigned short *a, const unsigned short *b, float *d);
+
 /* One call, host buffers in and out (reuses a cached session). */
 int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,
                   const particles *ptl_init, particles *ptl, int *nsteps_ptl,

@@ -33,6 +33,7 @@ UNITS = [
     ("track_surrogate.o", "track_surrogate.cu", ["-fmad=true", "-ftz=true"]),
     ("host_config.o", "host_config.cpp", ["-x", "cu"]),
     ("noalloc.o", "noalloc.cu", []),
+    ("tc_gemm.o", "tc_gemm.cu", []),
 ]
 
 

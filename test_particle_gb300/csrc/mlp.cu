@@ -354,6 +354,7 @@ struct MlpState {
     size_t woff[kLayers], boff[kLayers];
     float *p = nullptr, *gr = nullptr, *m = nullptr, *v = nullptr;
     __nv_bfloat16 *wb[kLayers] = {}, *wt[kLayers] = {};
+    unsigned char* wpack = nullptr;         // kPackBytes, tensor-core inference layout
     int* freq = nullptr;
     float out_mean[kOut] = {0}, out_std[kOut] = {1, 1, 1, 1, 1, 1};
     float *d_mean = nullptr, *d_istd = nullptr;
@@ -392,7 +393,8 @@ static bool mlp_alloc_params()
             !cuda_ok(cudaMalloc(&M.wt[l], sizeof(__nv_bfloat16) * e), "mlp wt"))
             return false;
     }
-    return cuda_ok(cudaMalloc(&M.freq, sizeof(int) * 3 * kFeat), "mlp freq") &&
+    return cuda_ok(cudaMalloc(&M.wpack, kPackBytes), "mlp wpack") &&
+           cuda_ok(cudaMalloc(&M.freq, sizeof(int) * 3 * kFeat), "mlp freq") &&
            cuda_ok(cudaMalloc(&M.d_mean, sizeof(float) * kOut), "mlp mean") &&
            cuda_ok(cudaMalloc(&M.d_istd, sizeof(float) * kOut), "mlp std") &&
            cuda_ok(cudaMalloc(&M.loss, sizeof(double)), "mlp loss");
@@ -424,6 +426,7 @@ static bool mlp_refresh_bf16()
         to_bf16_kernel<<<(e + 255) / 256, 256, 0, s>>>(M.p + M.woff[l], layer_out(l), layer_out_pad(l),
                                                        layer_in(l), M.wb[l], M.wt[l]);
     }
+    if (!cuda_ok(pack_weights(M.wb, M.wpack, s), "pack weights")) return false;
     float istd[kOut];
     for (int c = 0; c < kOut; c++) istd[c] = 1.0f / M.out_std[c];
     cudaMemcpyAsync(M.d_mean, M.out_mean, sizeof(float) * kOut, cudaMemcpyHostToDevice, s);
@@ -509,6 +512,7 @@ bool mlp::mlp_model(Model& md)
         md.b[l] = M.p + M.boff[l];
     }
     md.freq = M.freq;
+    md.wpack = M.wpack;
     for (int c = 0; c < kOut; c++) {
         md.out_scale[c] = M.out_std[c];
         md.out_shift[c] = M.out_mean[c];

@@ -24,11 +24,18 @@ struct Model {
     const __nv_bfloat16* w[kLayers];  // [out_pad][in] row-major, BF16
     const float* b[kLayers];          // [out] FP32
     const int* freq;                  // [kFeat][3] integer lattice frequencies
+    const unsigned char* wpack;       // weights in the tensor-core chunk layout (kPackBytes)
     float out_scale[kOut], out_shift[kOut];  // y = net * scale + shift
 };
 
+// Bytes of the packed weights: 32 chunks per evaluation (see track_surrogate.cu).
+constexpr size_t kPackBytes = 466944;
+
 // Device view of the trained model (host side; false and an error if untrained).
 bool mlp_model(Model& md);
+
+// Packs the BF16 weights of every layer for the tensor-core inference.
+cudaError_t pack_weights(const __nv_bfloat16* const w[kLayers], unsigned char* pack, cudaStream_t s);
 
 __device__ __forceinline__ float silu(float z)
 {

@@ -85,6 +85,7 @@ enum : int {
     ST_NONFINITE = 2,
     ST_STEP_LIMIT = 4,    // adaptive stepper hit its per-particle step cap
     ST_UNDERFLOW = 8,     // adaptive step size underflow
+    ST_TIMEOUT = 16,      // a bounded wait on the tensor-core pipeline gave up
 };
 
 }  // namespace tp

@@ -199,7 +199,7 @@ static cudaError_t launch_sys(const MixField& f, const TrackBufs& b, const Track
                               cudaStream_t s)
 {
     size_t smem = SYS == TP_SYS_MODESUM ? sizeof(ModeF) * (size_t)f.nmodes : 0;
-    if (smem > 48 * 1024) {
+    if (smem > 0) {  // static plus dynamic shared memory may pass the 48 KB default
         cudaError_t e = cudaFuncSetAttribute(track_mixed_kernel<SYS>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
@@ -230,7 +230,7 @@ int track_max_blocks_per_sm(int system_type, int nmodes)
     case TP_SYS_FORCEFREE: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, track_mixed_kernel<TP_SYS_FORCEFREE>, kBlock, 0); break;
     case TP_SYS_PIC: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, track_mixed_kernel<TP_SYS_PIC>, kBlock, 0); break;
     case TP_SYS_MODESUM:
-        if (smem > 48 * 1024)
+        if (smem > 0)
             cudaFuncSetAttribute(track_mixed_kernel<TP_SYS_MODESUM>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, track_mixed_kernel<TP_SYS_MODESUM>, kBlock, smem);

@@ -1,142 +1,277 @@
 // track_surrogate.cu -- tracking with the learned field model: the FP32 Wirz
-// push of the mixed path, with every field evaluation done for the 128
-// particles of a block at once as a chain of BF16 tensor-core GEMMs
-// (mma.sync m16n8k16, FP32 accumulation) through shared memory.
+// push of the mixed path, with every field evaluation done for the 256
+// particles of a block at once as a chain of BF16 GEMMs on the 5th-generation
+// tensor cores (tcgen05.mma, FP32 accumulators in tensor memory).
 //
-// Block layout: 4 warps, warp w owns rows [32w, 32w + 32) = its own 32
-// particles, so activations never cross warps; weights stream from L2 into a
-// shared chunk of 64 output neurons at a time and are shared by all warps.
+// Block layout: 256 threads = two 128-row tiles; thread t owns row t % 128 of
+// tile t / 128 (its particle), which is also the tensor-memory lane its warp
+// may read.  Activations live in shared memory as the MMA A operand (128-byte
+// swizzled, K-major), one 64 KB buffer per tile, rewritten in place by each
+// layer's epilogue.  Weights are pre-packed in the same layout as 32 chunks
+// per evaluation (16 KB: 128 output rows x 64 inputs; the output layer 2 KB)
+// and stream from L2 through a 4-stage ring of shared buffers by 1-D bulk
+// async copies; thread 0 issues the copies and the MMAs, tracking the ring
+// with mbarriers, and every wait on them is bounded.
 #include <cstring>
 
 #include "../../include/tp_gpu.h"
 #include "mlp_common.cuh"
+#include "tc_sm100.cuh"
 #include "tp_internal.h"
 #include "wirz_f32.cuh"
 
 namespace tp {
 namespace mlp {
 
-constexpr int kB = 128;            // particles (rows) per block
-constexpr int kLD = kHid + 8;      // activation row stride (bf16), conflict-free fragments
-constexpr int kWRows = 64;         // weight rows staged per chunk
-constexpr size_t kSmemH = sizeof(__nv_bfloat16) * kB * kLD;
-constexpr size_t kSmemW = sizeof(__nv_bfloat16) * kWRows * kLD;
-constexpr size_t kSmemY = sizeof(float) * kB * 8;
-constexpr size_t kSmemTotal = 2 * kSmemH + kSmemW + kSmemY;
+constexpr int kTiles = 2;
+constexpr int kB = 128 * kTiles;         // particles (threads) per block
+constexpr int kStages = 4;
+constexpr uint32_t kStageBytes = 16384;
+constexpr uint32_t kABytes = 128 * kHid * 2;  // one tile's activations (65536)
+constexpr int kChunks = 32;              // weight chunks per evaluation
+constexpr size_t kSmemDyn = 1024 + kTiles * kABytes + kStages * kStageBytes;
+constexpr int kSurrSmemBins = 1024;
+constexpr uint32_t kWaitLimit = 1u << 22;
+constexpr uint32_t kTmemCols = 256 * kTiles;
 
-struct Smem {
-    __nv_bfloat16* h0;
-    __nv_bfloat16* h1;
-    __nv_bfloat16* w;
-    float* y;
+// chunk j of an evaluation: layer, output half, k-atom, bytes and offset in the pack
+struct Chunk {
+    int layer, half, katom;
+    uint32_t bytes, offset;
 };
 
-// All 128 threads call this together; each passes its own position and
-// receives the model's E and B there.
-__device__ __noinline__ void field_block(const Model& md, const int* sfreq, const Smem& sm,
-                                         const uint64_t X[3], float E[3], float B[3])
+__host__ __device__ __forceinline__ Chunk chunk_of(int j)
 {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int g = lane >> 2, t = lane & 3;
-    // features of this thread's particle: row tid of h1
+    Chunk c;
+    if (j < 4) {
+        c.layer = 0; c.half = j >> 1; c.katom = j & 1;
+        c.bytes = kStageBytes; c.offset = (uint32_t)j * kStageBytes;
+    } else if (j < 28) {
+        const int jj = (j - 4) & 7;
+        c.layer = 1 + (j - 4) / 8; c.half = jj >> 2; c.katom = jj & 3;
+        c.bytes = kStageBytes; c.offset = 65536u + (uint32_t)(j - 4) * kStageBytes;
+    } else {
+        c.layer = 4; c.half = 0; c.katom = j - 28;
+        c.bytes = 2048; c.offset = 458752u + (uint32_t)(j - 28) * 2048u;
+    }
+    return c;
+}
+
+// byte offset in the pack of weight (n, k) of layer l (n < padded outputs)
+__host__ __device__ __forceinline__ uint32_t pack_offset(int l, int n, int k)
+{
+    if (l == kLayers - 1) return 458752u + (uint32_t)(k >> 6) * 2048u + tc::sw128_offset(16, n, k & 63);
+    const int ka = layer_in(l) / 64, h = n >> 7, a = k >> 6;
+    const uint32_t base = l == 0 ? 0u : 65536u + (uint32_t)(l - 1) * 131072u;
+    return base + (uint32_t)(h * ka + a) * kStageBytes + tc::sw128_offset(128, n & 127, k & 63);
+}
+
+// Shared state of the block's tensor-core pipeline.
+struct Pipe {
+    unsigned char* a[kTiles];        // activation tiles (A operands)
+    uint32_t stage0;                 // shared address of stage 0
+    uint32_t full, empty, done;      // mbarrier addresses (full/empty: kStages each, 8 B apart)
+    uint32_t tmem;
+    int* abort;
+    const float* bias;               // shared copy: 4 x 256 hidden biases then 6 output biases
+    const int* freq;
+    // thread 0 only: chunk counters (monotonic) and layer-completion count
+    uint32_t next_load, next_use, ndone;
+};
+
+__device__ __forceinline__ void issue_load(Pipe& pp, const unsigned char* wpack)
+{
+    const uint32_t c = pp.next_load;
+    const uint32_t s = c % kStages, use = c / kStages;
+    if (use > 0 && !tc::mbar_wait(pp.empty + 8 * s, (use - 1) & 1, kWaitLimit)) {
+        *pp.abort = 1;
+        return;
+    }
+    const Chunk ch = chunk_of((int)(c % kChunks));
+    tc::mbar_expect_tx(pp.full + 8 * s, ch.bytes);
+    tc::bulk_g2s(pp.stage0 + s * kStageBytes, wpack + ch.offset, ch.bytes, pp.full + 8 * s);
+    pp.next_load = c + 1;
+}
+
+// Thread 0: the MMAs of one layer (its chunks in sequence), refilling the
+// ring one chunk behind, then a commit to the layer barrier.
+__device__ void issue_layer(Pipe& pp, const unsigned char* wpack, int layer)
+{
+    const uint32_t idesc = tc::idesc_bf16_f32(128, layer == kLayers - 1 ? 16 : 128);
+    for (;;) {
+        const uint32_t c = pp.next_use;
+        const Chunk ch = chunk_of((int)(c % kChunks));
+        if (ch.layer != layer || *pp.abort) break;
+        const uint32_t s = c % kStages, use = c / kStages;
+        if (!tc::mbar_wait(pp.full + 8 * s, use & 1, kWaitLimit)) {
+            *pp.abort = 1;
+            break;
+        }
+        tc::tc_fence_after();
+        const uint32_t b0 = pp.stage0 + s * kStageBytes;
+#pragma unroll
+        for (int t = 0; t < kTiles; t++) {
+            const uint32_t a0 = tc::smem_addr(pp.a[t]) + (uint32_t)ch.katom * 128u * 128u;
+            const uint32_t d = pp.tmem + (uint32_t)(t * 256 + ch.half * 128);
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++)
+                tc::mma_bf16(d, tc::desc_sw128(a0 + kk * 32), tc::desc_sw128(b0 + kk * 32), idesc,
+                             (ch.katom | kk) != 0);
+        }
+        tc::mma_commit(pp.empty + 8 * s);
+        pp.next_use = c + 1;
+        // keep kStages - 1 chunks in flight: refill the stage the previous chunk used
+        while (pp.next_load < pp.next_use + kStages - 1 && !*pp.abort) issue_load(pp, wpack);
+    }
+    tc::mma_commit(pp.done);
+}
+
+// All kB threads call this together; each passes its own position and
+// receives the model's E and B there.  Returns zeros once the pipeline aborted.
+__device__ __noinline__ void field_block(const Model& md, Pipe& pp, const uint64_t X[3], float E[3],
+                                         float B[3])
+{
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tile = tid >> 7, row = tid & 127;
+    unsigned char* arow = pp.a[tile];
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    const uint32_t tcol = pp.tmem + lane_base + (uint32_t)(tile * 256);
+    // Fourier features of this thread's particle: inputs 0..63 sin, 64..127 cos
     {
-        __nv_bfloat16* xr = sm.h1 + tid * kLD;
-        uint32_t U0 = (uint32_t)(X[0] >> 32), U1 = (uint32_t)(X[1] >> 32), U2 = (uint32_t)(X[2] >> 32);
-        for (int j = 0; j < kFeat; j++) {
-            uint32_t ph = (uint32_t)sfreq[3 * j] * U0 + (uint32_t)sfreq[3 * j + 1] * U1 +
-                          (uint32_t)sfreq[3 * j + 2] * U2;
-            float s, c;
-            __sincosf(mixed::rev_to_rad(ph), &s, &c);
-            xr[j] = __float2bfloat16(s);
-            xr[kFeat + j] = __float2bfloat16(c);
+        const uint32_t U0 = (uint32_t)(X[0] >> 32), U1 = (uint32_t)(X[1] >> 32), U2 = (uint32_t)(X[2] >> 32);
+#pragma unroll 1
+        for (int j0 = 0; j0 < kFeat; j0 += 8) {
+            uint32_t ps[4], pc[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                float sv[2], cv[2];
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    const int j = j0 + 2 * q + e;
+                    const uint32_t ph = (uint32_t)pp.freq[3 * j] * U0 + (uint32_t)pp.freq[3 * j + 1] * U1 +
+                                        (uint32_t)pp.freq[3 * j + 2] * U2;
+                    __sincosf(mixed::rev_to_rad(ph), &sv[e], &cv[e]);
+                }
+                ps[q] = pack_bf16(sv[0], sv[1]);
+                pc[q] = pack_bf16(cv[0], cv[1]);
+            }
+            *reinterpret_cast<uint4*>(arow + tc::sw128_offset(128, row, j0)) = make_uint4(ps[0], ps[1], ps[2], ps[3]);
+            *reinterpret_cast<uint4*>(arow + tc::sw128_offset(128, row, kFeat + j0)) =
+                make_uint4(pc[0], pc[1], pc[2], pc[3]);
         }
     }
-    __syncwarp();
-    const __nv_bfloat16* hin = sm.h1;
-    __nv_bfloat16* hout = sm.h0;
+    tc::fence_async_smem();
+    tc::tc_fence_before();
+    __syncthreads();
     for (int l = 0; l < kLayers; l++) {
-        const int K = layer_in(l), Np = layer_out_pad(l);
-        const __nv_bfloat16* W = md.w[l];
-        const float* bias = md.b[l];
-        const bool last = l == kLayers - 1;
-        for (int nc = 0; nc < Np; nc += kWRows) {
-            const int nrows = Np - nc < kWRows ? Np - nc : kWRows;
-            __syncthreads();  // the weight chunk buffer is free
-            const int per_row = K / 8;
-            for (int c = tid; c < nrows * per_row; c += kB) {
-                int r = c / per_row, kk = (c - r * per_row) * 8;
-                *reinterpret_cast<uint4*>(sm.w + r * kLD + kk) =
-                    __ldg(reinterpret_cast<const uint4*>(W + (size_t)(nc + r) * K + kk));
-            }
-            __syncthreads();
-            float acc[2][8][4];
-#pragma unroll
-            for (int i = 0; i < 2; i++)
-#pragma unroll
-                for (int j = 0; j < 8; j++)
-#pragma unroll
-                    for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
-            const int ntl = nrows / 8;
-            for (int k0 = 0; k0 < K; k0 += 16) {
-                uint32_t af[2][4];
-#pragma unroll
-                for (int i = 0; i < 2; i++) {
-                    const __nv_bfloat16* r0 = hin + (warp * 32 + i * 16 + g) * kLD + k0 + 2 * t;
-                    af[i][0] = *reinterpret_cast<const uint32_t*>(r0);
-                    af[i][1] = *reinterpret_cast<const uint32_t*>(r0 + 8 * kLD);
-                    af[i][2] = *reinterpret_cast<const uint32_t*>(r0 + 8);
-                    af[i][3] = *reinterpret_cast<const uint32_t*>(r0 + 8 * kLD + 8);
-                }
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    if (j < ntl) {
-                        const __nv_bfloat16* wr = sm.w + (j * 8 + g) * kLD + k0 + 2 * t;
-                        uint32_t bfr[2] = {*reinterpret_cast<const uint32_t*>(wr),
-                                           *reinterpret_cast<const uint32_t*>(wr + 8)};
-                        mma_bf16(acc[0][j], af[0], bfr);
-                        mma_bf16(acc[1][j], af[1], bfr);
-                    }
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < 2; i++)
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    if (j >= ntl) continue;
-                    const int row = warp * 32 + i * 16 + g;
-                    const int col = nc + j * 8 + 2 * t;
-                    if (!last) {
-                        float b0 = __ldg(bias + col), b1 = __ldg(bias + col + 1);
-                        *reinterpret_cast<uint32_t*>(hout + row * kLD + col) =
-                            pack_bf16(silu(acc[i][j][0] + b0), silu(acc[i][j][1] + b1));
-                        *reinterpret_cast<uint32_t*>(hout + (row + 8) * kLD + col) =
-                            pack_bf16(silu(acc[i][j][2] + b0), silu(acc[i][j][3] + b1));
-                    } else {
-                        if (col < kOut) {
-                            sm.y[row * 8 + col] = acc[i][j][0] + __ldg(bias + col);
-                            sm.y[(row + 8) * 8 + col] = acc[i][j][2] + __ldg(bias + col);
-                        }
-                        if (col + 1 < kOut) {
-                            sm.y[row * 8 + col + 1] = acc[i][j][1] + __ldg(bias + col + 1);
-                            sm.y[(row + 8) * 8 + col + 1] = acc[i][j][3] + __ldg(bias + col + 1);
-                        }
-                    }
-                }
+        if (tid == 0) {
+            tc::tc_fence_after();
+            if (!*pp.abort) issue_layer(pp, md.wpack, l);
+            if (!*pp.abort && !tc::mbar_wait(pp.done, pp.ndone & 1, kWaitLimit)) *pp.abort = 1;
+            pp.ndone++;
         }
-        if (!last) {
-            const __nv_bfloat16* tmp = hin;
-            hin = hout;
-            hout = const_cast<__nv_bfloat16*>(tmp);
+        __syncthreads();
+        tc::tc_fence_after();
+        if (*pp.abort) {
+            E[0] = E[1] = E[2] = 0.f;
+            B[0] = B[1] = B[2] = 0.f;
+            return;
         }
+        if (l < kLayers - 1) {
+            const float* bias = pp.bias + l * kHid;
+#pragma unroll 1
+            for (int c0 = 0; c0 < kHid; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(tcol + (uint32_t)c0, v);
+                uint32_t pk[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    pk[q] = pack_bf16(silu(v[2 * q] + bias[c0 + 2 * q]), silu(v[2 * q + 1] + bias[c0 + 2 * q + 1]));
+                *reinterpret_cast<uint4*>(arow + tc::sw128_offset(128, row, c0)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                *reinterpret_cast<uint4*>(arow + tc::sw128_offset(128, row, c0 + 8)) =
+                    make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            }
+            tc::fence_async_smem();
+        } else {
+            float v[16];
+            tc::tmem_ld16(tcol, v);
+            const float* bo = pp.bias + (kLayers - 1) * kHid;
+            B[0] = (v[0] + bo[0]) * md.out_scale[0] + md.out_shift[0];
+            B[1] = (v[1] + bo[1]) * md.out_scale[1] + md.out_shift[1];
+            B[2] = (v[2] + bo[2]) * md.out_scale[2] + md.out_shift[2];
+            E[0] = (v[3] + bo[3]) * md.out_scale[3] + md.out_shift[3];
+            E[1] = (v[4] + bo[4]) * md.out_scale[4] + md.out_shift[4];
+            E[2] = (v[5] + bo[5]) * md.out_scale[5] + md.out_shift[5];
+        }
+        tc::tc_fence_before();
+        __syncthreads();
     }
-    __syncwarp();
-    const float* yr = sm.y + tid * 8;
-    B[0] = yr[0] * md.out_scale[0] + md.out_shift[0];
-    B[1] = yr[1] * md.out_scale[1] + md.out_shift[1];
-    B[2] = yr[2] * md.out_scale[2] + md.out_shift[2];
-    E[0] = yr[3] * md.out_scale[3] + md.out_shift[3];
-    E[1] = yr[4] * md.out_scale[4] + md.out_shift[4];
-    E[2] = yr[5] * md.out_scale[5] + md.out_shift[5];
+}
+
+// Block set-up shared by the kernels: shared layout, biases and frequencies,
+// mbarriers, tensor memory, and the first chunks in flight.
+struct SmemStatic {
+    float bias[kLayers * kHid];
+    int freq[3 * kFeat];
+    uint64_t bars[2 * kStages + 1];
+    uint32_t tmem_slot;
+    int abort;
+};
+
+__device__ void pipe_setup(Pipe& pp, SmemStatic& st, unsigned char* dyn, const Model& md)
+{
+    const int tid = threadIdx.x;
+    const uint32_t raw = tc::smem_addr(dyn);
+    unsigned char* base = dyn + ((1024u - (raw & 1023u)) & 1023u);
+    for (int t = 0; t < kTiles; t++) pp.a[t] = base + t * kABytes;
+    pp.stage0 = tc::smem_addr(base + kTiles * kABytes);
+    for (int k = tid; k < (kLayers - 1) * kHid; k += blockDim.x) st.bias[k] = md.b[k / kHid][k % kHid];
+    if (tid < kOut) st.bias[(kLayers - 1) * kHid + tid] = md.b[kLayers - 1][tid];
+    for (int k = tid; k < 3 * kFeat; k += blockDim.x) st.freq[k] = md.freq[k];
+    pp.full = tc::smem_addr(&st.bars[0]);
+    pp.empty = tc::smem_addr(&st.bars[kStages]);
+    pp.done = tc::smem_addr(&st.bars[2 * kStages]);
+    pp.abort = &st.abort;
+    pp.bias = st.bias;
+    pp.freq = st.freq;
+    pp.next_load = pp.next_use = pp.ndone = 0;
+    if (tid == 0) {
+        st.abort = 0;
+        for (int s = 0; s < kStages; s++) {
+            tc::mbar_init(pp.full + 8 * s, 1);
+            tc::mbar_init(pp.empty + 8 * s, 1);
+        }
+        tc::mbar_init(pp.done, 1);
+        tc::mbar_fence_init();
+    }
+    if ((tid >> 5) == 0) {
+        tc::tmem_alloc(tc::smem_addr(&st.tmem_slot), kTmemCols);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    pp.tmem = st.tmem_slot;
+    if (tid == 0)
+        while (pp.next_load < (uint32_t)(kStages - 1)) issue_load(pp, md.wpack);
+}
+
+// Waits (bounded) for the copies still in flight, then frees tensor memory.
+__device__ void pipe_teardown(Pipe& pp, int* status)
+{
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        bool ok = !*pp.abort;
+        for (uint32_t c = pp.next_use; c < pp.next_load; c++) {
+            const uint32_t s = c % kStages, use = c / kStages;
+            if (!tc::mbar_wait(pp.full + 8 * s, use & 1, kWaitLimit)) ok = false;
+        }
+        if (!ok) atomicOr(status, ST_TIMEOUT);
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    if ((tid >> 5) == 0) tc::tmem_dealloc(pp.tmem, kTmemCols);
 }
 
 // Fixed-step tracking with the learned field (src/tracking.c:297-462
@@ -147,21 +282,17 @@ __global__ void __launch_bounds__(kB, 1) track_surrogate_kernel(mixed::MixField 
                                                                  TrackBufs b, TrackParams q)
 {
     using namespace mixed;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(1024) unsigned char smem_dyn[];
+    __shared__ SmemStatic st;
     __shared__ double red[(kB / 32) * 8];
-    __shared__ unsigned int hist[kMaxSmemBins];
-    __shared__ int sfreq[3 * kFeat];
-    Smem sm;
-    sm.h0 = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-    sm.h1 = reinterpret_cast<__nv_bfloat16*>(smem_raw + kSmemH);
-    sm.w = reinterpret_cast<__nv_bfloat16*>(smem_raw + 2 * kSmemH);
-    sm.y = reinterpret_cast<float*>(smem_raw + 2 * kSmemH + kSmemW);
-    for (int k = threadIdx.x; k < 3 * kFeat; k += blockDim.x) sfreq[k] = md.freq[k];
-    __syncthreads();
-    const bool smem_hist = q.nbins <= kMaxSmemBins;
+    __shared__ unsigned int hist[kSurrSmemBins];
+    Pipe pp;
+    pipe_setup(pp, st, smem_dyn, md);
+    const bool smem_hist = q.nbins <= kSurrSmemBins;
     const float dt = (float)q.dt;
-    auto field = [&](const uint64_t* X, float* E, float* B) { field_block(md, sfreq, sm, X, E, B); };
-    for (int tile = blockIdx.x; tile < q.ntiles; tile += gridDim.x) {
+    const int ntiles = (q.n + kB - 1) / kB;
+    auto field = [&](const uint64_t* X, float* E, float* B) { field_block(md, pp, X, E, B); };
+    for (int tile = blockIdx.x; tile < ntiles && !st.abort; tile += gridDim.x) {
         const int i = tile * kB + threadIdx.x;
         const bool active = i < q.n;
         PM p = {};
@@ -207,7 +338,7 @@ __global__ void __launch_bounds__(kB, 1) track_surrogate_kernel(mixed::MixField 
         int to_diff = kDiffInterval - q.sstep % kDiffInterval;
         if (to_frame == q.einterval) to_frame = 0;
         if (to_diff == kDiffInterval) to_diff = 0;
-        for (int j = q.sstep; j <= q.estep; j++) {
+        for (int j = q.sstep; j <= q.estep && !st.abort; j++) {
             const bool at_diff = to_diff == 0, at_frame = to_frame == 0;
             to_diff = at_diff ? kDiffInterval - 1 : to_diff - 1;
             to_frame = at_frame ? q.einterval - 1 : to_frame - 1;
@@ -277,7 +408,7 @@ __global__ void __launch_bounds__(kB, 1) track_surrogate_kernel(mixed::MixField 
             if (active && esc_after && at_diff && tstep < q.nsdc) atomicSub(&b.remain[tstep], 1);
             esc_pre = esc_after;
         }
-        if (active) {
+        if (active && !st.abort) {
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 double xk = f.min[k] + f.L[k] * ((double)p.X[k] * 5.421010862427522e-20);
@@ -292,43 +423,64 @@ __global__ void __launch_bounds__(kB, 1) track_surrogate_kernel(mixed::MixField 
         }
         __syncthreads();
     }
+    pipe_teardown(pp, b.status);
 }
 
 // Model field at n positions through the in-kernel (per-block) evaluation path.
 __global__ void __launch_bounds__(kB, 1) field_eval_kernel(Model md, const uint32_t* __restrict__ U,
-                                                           int n, float* __restrict__ out)
+                                                           int n, float* __restrict__ out, int* status)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ int sfreq[3 * kFeat];
-    Smem sm;
-    sm.h0 = reinterpret_cast<__nv_bfloat16*>(smem_raw);
-    sm.h1 = reinterpret_cast<__nv_bfloat16*>(smem_raw + kSmemH);
-    sm.w = reinterpret_cast<__nv_bfloat16*>(smem_raw + 2 * kSmemH);
-    sm.y = reinterpret_cast<float*>(smem_raw + 2 * kSmemH + kSmemW);
-    for (int k = threadIdx.x; k < 3 * kFeat; k += blockDim.x) sfreq[k] = md.freq[k];
-    __syncthreads();
-    for (int tile = blockIdx.x; tile * kB < n; tile += gridDim.x) {
+    extern __shared__ __align__(1024) unsigned char smem_dyn[];
+    __shared__ SmemStatic st;
+    Pipe pp;
+    pipe_setup(pp, st, smem_dyn, md);
+    for (int tile = blockIdx.x; tile * kB < n && !st.abort; tile += gridDim.x) {
         int i = tile * kB + threadIdx.x;
         uint64_t X[3] = {0, 0, 0};
         if (i < n)
             for (int k = 0; k < 3; k++) X[k] = (uint64_t)U[3 * i + k] << 32;
         float E[3], B[3];
-        field_block(md, sfreq, sm, X, E, B);
-        if (i < n) {
+        field_block(md, pp, X, E, B);
+        if (i < n && !st.abort) {
             out[6 * i] = B[0]; out[6 * i + 1] = B[1]; out[6 * i + 2] = B[2];
             out[6 * i + 3] = E[0]; out[6 * i + 4] = E[1]; out[6 * i + 5] = E[2];
         }
-        __syncthreads();
     }
+    pipe_teardown(pp, status);
+}
+
+// Packs the BF16 weights [out_pad][in] of every layer into the chunk layout above.
+__global__ void pack_weights_kernel(const __nv_bfloat16* w0, const __nv_bfloat16* w1, const __nv_bfloat16* w2,
+                                    const __nv_bfloat16* w3, const __nv_bfloat16* w4, unsigned char* pack)
+{
+    const __nv_bfloat16* ws[kLayers] = {w0, w1, w2, w3, w4};
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int l = 0; l < kLayers; l++) {
+        const int n_elem = layer_out_pad(l) * layer_in(l);
+        if (i < n_elem) {
+            const int n = i / layer_in(l), k = i % layer_in(l);
+            *reinterpret_cast<__nv_bfloat16*>(pack + pack_offset(l, n, k)) = ws[l][i];
+            return;
+        }
+        i -= n_elem;
+    }
+}
+
+cudaError_t pack_weights(const __nv_bfloat16* const w[kLayers], unsigned char* pack, cudaStream_t s)
+{
+    int total = 0;
+    for (int l = 0; l < kLayers; l++) total += layer_out_pad(l) * layer_in(l);
+    pack_weights_kernel<<<(total + 255) / 256, 256, 0, s>>>(w[0], w[1], w[2], w[3], w[4], pack);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_track_surrogate(const mixed::MixField& f, const Model& md, const TrackBufs& b,
                                    const TrackParams& q, int grid, cudaStream_t s)
 {
     cudaError_t e = cudaFuncSetAttribute(track_surrogate_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTotal);
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDyn);
     if (e != cudaSuccess) return e;
-    track_surrogate_kernel<<<grid, kB, kSmemTotal, s>>>(f, md, b, q);
+    track_surrogate_kernel<<<grid, kB, kSmemDyn, s>>>(f, md, b, q);
     return cudaGetLastError();
 }
 
@@ -350,11 +502,11 @@ extern "C" int tp_mlp_eval_kernel(int n, const unsigned int* u, float* out6)
     cudaStream_t s = g.stream;
     cudaMemcpyAsync(dU, u, sizeof(uint32_t) * 3 * n, cudaMemcpyHostToDevice, s);
     bool ok = cuda_ok(cudaFuncSetAttribute(mlp::field_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)mlp::kSmemTotal), "smem attr");
+                                           (int)mlp::kSmemDyn), "smem attr");
     if (ok) {
         int grid = (n + mlp::kB - 1) / mlp::kB;
         if (grid > g.num_sms) grid = g.num_sms;
-        mlp::field_eval_kernel<<<grid, mlp::kB, mlp::kSmemTotal, s>>>(md, dU, n, dO);
+        mlp::field_eval_kernel<<<grid, mlp::kB, mlp::kSmemDyn, s>>>(md, dU, n, dO, g.d_status);
         ok = cuda_ok(cudaGetLastError(), "field eval");
     }
     if (ok) {

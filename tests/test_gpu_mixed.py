@@ -34,15 +34,18 @@ def setup(kind, steps, n=8192, seed=5):
         cfg = wl.config_modesum(nptl=n, steps=steps)
         dom.xmax = dom.ymax = dom.zmax = 1.0
         dom.tmax = steps * cfg["dt"] + 0.5 * cfg["dt"]
-        modes = wl.kolmogorov_modes(128, 1, 16, 1.0, seed, va=0.1)
+        # 512 modes: the mode table alone takes 22 KB of shared memory
+        nm, kmax = (512, 64) if kind == "modesum512" else (128, 16)
+        modes = wl.kolmogorov_modes(nm, 1, kmax, 1.0, seed, va=0.1)
         tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=1.0)
     tp.set_spectrum(200, 1e-3, 1e2)
     p0 = wl.shell_particles(n, 0.7, cfg["lo"], cfg["hi"], seed)
     return cfg, p0
 
 
-@pytest.mark.parametrize("kind", ["abc", "grid", "modesum"])
-@pytest.mark.parametrize("steps,tol", [(1, 1e-5), (10, 1e-4)])
+@pytest.mark.parametrize("kind,steps,tol", [(k, s, t) for k in ("abc", "grid", "modesum")
+                                            for s, t in ((1, 1e-5), (10, 1e-4))] +
+                         [("modesum512", 1, 1e-5)])
 def test_mixed_short_horizon_per_particle(kind, steps, tol):
     """Before chaos amplifies FP32 rounding (the mode-sum field decorrelates
     within a few tens of steps) each particle follows the FP64 path."""

@@ -106,3 +106,32 @@ def test_surrogate_tracking_runs_and_tracks_the_exact_field():
     sa, sb = a["espect"] / 4096, b["espect"] / 4096
     assert np.all(np.abs(sa - sb).sum(axis=1) < 0.5)
     assert tp.device_status() == 0
+
+
+def test_tensor_core_inference_matches_fp64_forward():
+    """The in-kernel evaluation (tcgen05.mma chain, BF16 weights and
+    activations, FP32 accumulation in tensor memory) against the FP64 forward
+    pass of the same BF16 weights, on 3 tiles of 256 positions plus a ragged
+    tail."""
+    freq = lattice_freq(7)
+    tp.mlp_init(freq, seed=13)
+    tp.mlp_set_output_norm(np.zeros(6), np.ones(6))
+    w = tp.mlp_weights().astype(np.float64)
+    off = 0
+    for i, o in mo.SIZES:
+        w[off:off + i * o] = bf16_round(w[off:off + i * o])
+        off += i * o + o
+    rng = np.random.default_rng(17)
+    u = rng.integers(0, 2 ** 32, size=(3 * 256 + 77, 3), dtype=np.uint64).astype(np.uint32)
+    x = bf16_round(mo.features(u, freq)).astype(np.float64)
+    ref, _, _ = mo.forward(mo.unflatten(w), x)
+    got = tp.mlp_eval_kernel(u)
+    scale = np.abs(ref).max()
+    assert scale > 0
+    err = np.abs(got - ref).max() / scale
+    assert err < 3e-2, err
+    c = np.corrcoef(got.ravel(), ref.ravel())[0, 1]
+    assert c > 0.999, c
+    gemm = tp.mlp_eval(u)
+    assert np.abs(got - gemm).max() < 2e-2 * scale
+    assert tp.device_status() == 0
