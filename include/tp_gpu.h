@@ -117,6 +117,15 @@ void getemf_wlcs(double x, double y, double z, double t, struct emfields *emf_to
 void free_config(void);                                                                /* :227-229 */
 void adjust_dt_normI(double *dt);                                                      /* :266-269 */
 
+/* --- Poincare map (include/poincare_map.h, src/poincare_map.c) --- */
+/* src/poincare_map.c:39-239: reads the "Poincare map configuration" section,
+ * traces this rank's seeds on the GPU and writes the crossings through
+ * tp_poincare_save (Part 2). */
+int poincare_map(int mpi_rank, int mpi_size, char *config_file_name, domain *sdomain);
+extern int map_for_single_point, face_cross_section, nhorizontal, nvertical, ncross;
+extern double fx0, fy0, fz0, min_horizontal, max_horizontal, min_vertical, max_vertical;
+extern double step_fieldline, fieldline_length_max;
+
 /* --- gridded fields (include/{magnetic,electric,velocity}_field.h) --- */
 void set_variables_bfield(grids *sgrid, domain *sdomain, double B0_field, int mt, int dtype); /* magnetic_field.c:55-63 */
 void initialize_bfield(void);                                                          /* magnetic_field.c:102-116 */
@@ -270,6 +279,19 @@ int tp_mlp_eval_kernel(int n, const unsigned int *u, float *out6);
  * D[128][n]; n a multiple of 16 in [16, 256], k a multiple of 64 in
  * [64, 256].  A self-check of the tensor-core path of the learned field model. */
 int tp_tc_gemm_bf16(int n, int k, const unsigned short *a, const unsigned short *b, float *d);
+
+/* Field lines of the gridded B (system types 3 and 4) from n seeds [n][3],
+ * RK4 steps of length `step` on the unit vector of B, up to length_max in
+ * all; xpos/ypos/zpos [n][ncross + 1] get the seed and the first ncross
+ * crossings of the plane pos[face] = seed[face] (unreached entries: 2 * the
+ * box maximum of the axis); found[n] the crossings reached.  The tracing of
+ * src/poincare_map.c:101-181 for a batch of seeds. */
+int tp_poincare_trace(int n, const double *seeds, int face, double step, double length_max, int ncross,
+                      double *xpos, double *ypos, double *zpos, int *found);
+/* Writer used by poincare_map (weak; the default writes data/poincare_map.bin,
+ * see poincare.cu).  Define it to write the reference's HDF5 file instead. */
+void tp_poincare_save(int mpi_rank, int mpi_size, int npoints_total, int ncross, int nshift,
+                      int npoints, const double *xpos, const double *ypos, const double *zpos);
 
 /* One call, host buffers in and out (reuses a cached session). */
 int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,

@@ -22,7 +22,7 @@ COMMON=(-O2 -fPIC -fopenmp -fcommon -std=gnu99 -ffp-contract=off -w
         -I"$HERE/stubs" -I"$REF/include")
 SRCS=(tracking emfields force_free wlcs interpolation magnetic_field
       electric_field velocity_field diagnostics quick_sort particle_info
-      data_io bessel domain)
+      data_io bessel domain poincare_map)
 pids=()
 for s in "${SRCS[@]}"; do
   extra=(-include stdbool.h)

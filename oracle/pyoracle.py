@@ -286,3 +286,30 @@ def bs_run_many(f, y0, h0, nsteps, atol=1e-10, rtol=1e-10, kmaxx=8, nthreads=0):
     y = np.ascontiguousarray(y0, dtype=np.float64).copy()
     return oracle().or_bs_run_many(C.byref(f), C.byref(cfg), C.c_int(len(y)), ptr(y), C.c_double(h0),
                                    C.c_int(nsteps), C.c_int(nthreads))
+
+
+def next_location_steps(f, seeds, step, nsteps):
+    """nsteps RK4 field-line steps of the restatement from each seed; [n][nsteps][3]."""
+    lib = oracle()
+    s = np.ascontiguousarray(seeds, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros((len(s), nsteps, 3))
+    for i in range(len(s)):
+        x, y, z = C.c_double(s[i, 0]), C.c_double(s[i, 1]), C.c_double(s[i, 2])
+        for k in range(nsteps):
+            lib.or_next_location(C.byref(f), C.byref(x), C.byref(y), C.byref(z), C.c_double(step))
+            out[i, k] = (x.value, y.value, z.value)
+    return out
+
+
+def poincare(f, seeds, face, step, length_max, ncross, nthreads=0):
+    """Crossing points of every seed: (xpos, ypos, zpos) [n][ncross+1] and counts."""
+    s = np.ascontiguousarray(seeds, dtype=np.float64).reshape(-1, 3)
+    n = len(s)
+    xo = np.zeros((n, ncross + 1))
+    yo = np.zeros((n, ncross + 1))
+    zo = np.zeros((n, ncross + 1))
+    found = np.zeros(n, dtype=np.int32)
+    oracle().or_poincare_many(C.byref(f), C.c_int(n), ptr(s), C.c_int(face), C.c_double(step),
+                              C.c_double(length_max), C.c_int(ncross), ptr(xo), ptr(yo), ptr(zo),
+                              ptr(found), C.c_int(nthreads))
+    return xo, yo, zo, found

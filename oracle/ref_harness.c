@@ -16,6 +16,7 @@
  *   ellint / getemf_wlcs                               src/wlcs.c:460-865
  *   ptl_energy_fixed / calc_diff_coeff                 src/diagnostics.c:187-205,659-705
  *   StepperBase / step                                 src/unused/StepperBS.c:103-354
+ *   next_location                                      src/poincare_map.c:243-290
  */
 #include <math.h>
 #include <omp.h>
@@ -280,4 +281,22 @@ int refh_bs_integrate(double *y, double t0, double h0, int nsteps, double *out)
 void refh_derivs(double t, double *y, double *dydx)
 {
     derivs(t, y, dydx);
+}
+
+/* ---------------------------------------------------------------- Poincare
+ * next_location is the RK4 field-line step of src/poincare_map.c:243-290
+ * (not declared in the reference's headers). */
+void next_location(double *fx, double *fy, double *fz, double dstep);
+
+/* nsteps reference RK4 steps from each of n seeds; out[n][nsteps][3] */
+void refh_next_location(int n, const double *xyz, double step, int nsteps, double *out)
+{
+    for (int i = 0; i < n; i++) {
+        double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        for (int s = 0; s < nsteps; s++) {
+            next_location(&x, &y, &z, step);
+            double *o = out + ((size_t)i * nsteps + s) * 3;
+            o[0] = x; o[1] = y; o[2] = z;
+        }
+    }
 }

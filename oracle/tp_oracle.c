@@ -978,3 +978,108 @@ long or_bs_run_many(const or_field *f, const or_bs_cfg *cfg, int n, double *y, d
 #endif
     return total;
 }
+
+/* ------------------------------------------------------------ Poincare map
+ * src/poincare_map.c: field lines dx/|B| traced with fixed-step RK4 on the
+ * unit vector of B from get_magnetic_field (systems 3 and 4: the float B
+ * grid, src/emfields.c:76-96,122-188), periodic wrap of the evaluation points
+ * only (field_boundary, :296-321, applied to the input of every stage), and
+ * crossings of the plane pos[face] = seed[face] detected by a sign change of
+ * (pre - init) * (cur - init) (:101-118, :165-181). */
+static void or_field_boundary(const or_field *f, double *fx, double *fy, double *fz)
+{
+    double xdim = f->dom.xmax - f->dom.xmin, ydim = f->dom.ymax - f->dom.ymin;
+    double zdim = f->dom.zmax - f->dom.zmin;
+    if (*fx > f->dom.xmax) *fx -= xdim;
+    if (*fy > f->dom.ymax) *fy -= ydim;
+    if (*fz > f->dom.zmax) *fz -= zdim;
+    if (*fx < f->dom.xmin) *fx += xdim;
+    if (*fy < f->dom.ymin) *fy += ydim;
+    if (*fz < f->dom.zmin) *fz += zdim;
+}
+
+static void or_unit_b(const or_field *f, double x, double y, double z, double b[3])
+{
+    emfields e;
+    or_get_emf(f, x, y, z, 0, &e);  /* B part = get_bfield_{mhd,pic}_test_particle */
+    double ib = 1.0 / sqrt(e.Bx * e.Bx + e.By * e.By + e.Bz * e.Bz);
+    b[0] = e.Bx * ib;
+    b[1] = e.By * ib;
+    b[2] = e.Bz * ib;
+}
+
+/* next_location, src/poincare_map.c:243-290 */
+void or_next_location(const or_field *f, double *fx, double *fy, double *fz, double dstep)
+{
+    double b1[3], b2[3], b3[3], b4[3], xt, yt, zt;
+    or_field_boundary(f, fx, fy, fz);
+    or_unit_b(f, *fx, *fy, *fz, b1);
+    xt = *fx + 0.5 * dstep * b1[0];
+    yt = *fy + 0.5 * dstep * b1[1];
+    zt = *fz + 0.5 * dstep * b1[2];
+    or_field_boundary(f, &xt, &yt, &zt);
+    or_unit_b(f, xt, yt, zt, b2);
+    xt = *fx + 0.5 * dstep * b2[0];
+    yt = *fy + 0.5 * dstep * b2[1];
+    zt = *fz + 0.5 * dstep * b2[2];
+    or_field_boundary(f, &xt, &yt, &zt);
+    or_unit_b(f, xt, yt, zt, b3);
+    xt = *fx + dstep * b3[0];
+    yt = *fy + dstep * b3[1];
+    zt = *fz + dstep * b3[2];
+    or_field_boundary(f, &xt, &yt, &zt);
+    or_unit_b(f, xt, yt, zt, b4);
+    *fx += (dstep / 6) * (b1[0] + 2 * b2[0] + 2 * b3[0] + b4[0]);
+    *fy += (dstep / 6) * (b1[1] + 2 * b2[1] + 2 * b3[1] + b4[1]);
+    *fz += (dstep / 6) * (b1[2] + 2 * b2[2] + 2 * b3[2] + b4[2]);
+}
+
+/* The crossing loop of one seed (src/poincare_map.c:158-181): pos_out[3][ncross+1]
+ * (x row, y row, z row; entry 0 the seed), returns the crossings found. */
+int or_poincare_point(const or_field *f, const double seed[3], int face, double step,
+                      double length_max, int ncross, double *xo, double *yo, double *zo)
+{
+    double pos[3] = {seed[0], seed[1], seed[2]};
+    double init = seed[face];
+    xo[0] = seed[0]; yo[0] = seed[1]; zo[0] = seed[2];
+    int icross = 1;
+    double length = 0.0;
+    while (icross <= ncross) {
+        double cross = 1.0;
+        while (cross > 0 && length < length_max) {
+            double pre = pos[face];
+            or_next_location(f, &pos[0], &pos[1], &pos[2], step);
+            cross = (pre - init) * (pos[face] - init);
+            length += step;
+        }
+        if (length < length_max) {
+            xo[icross] = pos[0];
+            yo[icross] = pos[1];
+            zo[icross] = pos[2];
+            ++icross;
+        } else {
+            break;
+        }
+    }
+    return icross - 1;
+}
+
+/* Every seed (OpenMP); outputs [n][ncross+1] per coordinate, entries a seed
+ * did not reach keep the reference's fill value 2 * max of that axis. */
+void or_poincare_many(const or_field *f, int n, const double *seeds, int face, double step,
+                      double length_max, int ncross, double *xpos, double *ypos, double *zpos,
+                      int *found, int nthreads)
+{
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < n; i++) {
+        double *xo = xpos + (size_t)i * (ncross + 1), *yo = ypos + (size_t)i * (ncross + 1);
+        double *zo = zpos + (size_t)i * (ncross + 1);
+        for (int k = 0; k <= ncross; k++) {
+            xo[k] = f->dom.xmax * 2;
+            yo[k] = f->dom.ymax * 2;
+            zo[k] = f->dom.zmax * 2;
+        }
+        found[i] = or_poincare_point(f, seeds + 3 * i, face, step, length_max, ncross, xo, yo, zo);
+    }
+}

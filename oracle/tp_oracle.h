@@ -101,6 +101,14 @@ void or_bs_derivs(const or_field *f, double t, const double *y, double *dydx);
 long or_bs_run_many(const or_field *f, const or_bs_cfg *cfg, int n, double *y, double h0,
                     int nsteps, int nthreads);
 
+/* Poincare map, src/poincare_map.c */
+void or_next_location(const or_field *f, double *fx, double *fy, double *fz, double dstep);
+int or_poincare_point(const or_field *f, const double seed[3], int face, double step,
+                      double length_max, int ncross, double *xo, double *yo, double *zo);
+void or_poincare_many(const or_field *f, int n, const double *seeds, int face, double step,
+                      double length_max, int ncross, double *xpos, double *ypos, double *zpos,
+                      int *found, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

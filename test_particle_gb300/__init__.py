@@ -365,3 +365,19 @@ class Session:
             self.close()
         except Exception:
             pass
+
+
+def poincare_trace(seeds, face, step, length_max, ncross):
+    """Crossings of the plane pos[face] = seed[face] by the field lines of the
+    gridded B through each seed (tp_poincare_trace): xpos, ypos, zpos
+    [n][ncross + 1] (entry 0 the seed) and the crossings reached per seed."""
+    s = np.ascontiguousarray(seeds, dtype=np.float64).reshape(-1, 3)
+    n = len(s)
+    xo = np.zeros((n, ncross + 1))
+    yo = np.zeros((n, ncross + 1))
+    zo = np.zeros((n, ncross + 1))
+    found = np.zeros(n, dtype=np.int32)
+    check(lib().tp_poincare_trace(C.c_int(n), _ptr(s), C.c_int(face), C.c_double(step),
+                                  C.c_double(length_max), C.c_int(ncross), _ptr(xo), _ptr(yo),
+                                  _ptr(zo), _ptr(found)), "poincare_trace")
+    return xo, yo, zo, found

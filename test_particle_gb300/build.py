@@ -34,6 +34,7 @@ UNITS = [
     ("host_config.o", "host_config.cpp", ["-x", "cu"]),
     ("noalloc.o", "noalloc.cu", []),
     ("tc_gemm.o", "tc_gemm.cu", []),
+    ("poincare.o", "poincare.cu", []),
 ]
 
 

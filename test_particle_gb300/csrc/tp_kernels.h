@@ -24,6 +24,9 @@ namespace tp {
     cudaError_t launch_bc(const DevField& f, int n, double* st, int* iescape, cudaStream_t s); \
     cudaError_t launch_point_interp(const DevField& f, int which, int n, const double* xyzt,   \
                                     double* out, int* status, cudaStream_t s);                 \
+    cudaError_t launch_poincare(const DevField& f, int n, const double* seeds, int face,       \
+                                double h, double lmax, int ncross, double* xo, double* yo,     \
+                                double* zo, int* found, int* status, cudaStream_t s);          \
     }
 
 TP_DECLARE_FP64_LAUNCHERS(fp64)

@@ -429,6 +429,113 @@ __global__ void point_interp_kernel(DevField f, int which, int n, const double* 
     }
 }
 
+// ---------------------------------------------------------------- Poincare map
+// Field lines of the gridded B (get_magnetic_field, src/emfields.c:76-96:
+// the float B grid for systems 3 and 4) traced with the fixed-step RK4 of
+// next_location (src/poincare_map.c:243-290) on the unit vector of B, the
+// stage points wrapped into the box (field_boundary, :296-321), and the
+// crossings of the plane pos[face] = seed[face] recorded as the first point
+// after a sign change (:158-181).  One thread per seed.
+__device__ __forceinline__ void pm_boundary(const DevField& f, double& x, double& y, double& z)
+{
+    double xdim = f.xmax - f.xmin, ydim = f.ymax - f.ymin, zdim = f.zmax - f.zmin;
+    if (x > f.xmax) x -= xdim;
+    if (y > f.ymax) y -= ydim;
+    if (z > f.zmax) z -= zdim;
+    if (x < f.xmin) x += xdim;
+    if (y < f.ymin) y += ydim;
+    if (z < f.zmin) z += zdim;
+}
+
+__device__ __forceinline__ void pm_unit_b(const DevField& f, double x, double y, double z, double b[3],
+                                          int* status)
+{
+    Tri64 r;
+    trilinear64(f, x, y, z, 0.0, r);
+    float v[3];
+    interp_f3(f, r, f.bc_f, f.ba_f, f.bb_f, v, status);
+    double bx = v[0], by = v[1], bz = v[2];
+    double ib = 1.0 / sqrt(bx * bx + by * by + bz * bz);
+    b[0] = bx * ib;
+    b[1] = by * ib;
+    b[2] = bz * ib;
+}
+
+__device__ __forceinline__ void pm_next(const DevField& f, double& px, double& py, double& pz, double h,
+                                        int* status)
+{
+    double b1[3], b2[3], b3[3], b4[3], xt, yt, zt;
+    pm_boundary(f, px, py, pz);
+    pm_unit_b(f, px, py, pz, b1, status);
+    xt = px + 0.5 * h * b1[0];
+    yt = py + 0.5 * h * b1[1];
+    zt = pz + 0.5 * h * b1[2];
+    pm_boundary(f, xt, yt, zt);
+    pm_unit_b(f, xt, yt, zt, b2, status);
+    xt = px + 0.5 * h * b2[0];
+    yt = py + 0.5 * h * b2[1];
+    zt = pz + 0.5 * h * b2[2];
+    pm_boundary(f, xt, yt, zt);
+    pm_unit_b(f, xt, yt, zt, b3, status);
+    xt = px + h * b3[0];
+    yt = py + h * b3[1];
+    zt = pz + h * b3[2];
+    pm_boundary(f, xt, yt, zt);
+    pm_unit_b(f, xt, yt, zt, b4, status);
+    px += (h / 6) * (b1[0] + 2 * b2[0] + 2 * b3[0] + b4[0]);
+    py += (h / 6) * (b1[1] + 2 * b2[1] + 2 * b3[1] + b4[1]);
+    pz += (h / 6) * (b1[2] + 2 * b2[2] + 2 * b3[2] + b4[2]);
+}
+
+// outputs [n][ncross + 1] per coordinate; entries a seed does not reach keep
+// the reference's fill value 2 * max of the axis
+__global__ void poincare_kernel(DevField f, int n, const double* __restrict__ seeds, int face, double h,
+                                double lmax, int ncross, double* xo, double* yo, double* zo, int* found,
+                                int* status)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t row = (size_t)i * (ncross + 1);
+    for (int k = 0; k <= ncross; k++) {
+        xo[row + k] = f.xmax * 2;
+        yo[row + k] = f.ymax * 2;
+        zo[row + k] = f.zmax * 2;
+    }
+    double pos[3] = {seeds[3 * i], seeds[3 * i + 1], seeds[3 * i + 2]};
+    const double init = pos[face];
+    xo[row] = pos[0]; yo[row] = pos[1]; zo[row] = pos[2];
+    int icross = 1;
+    double length = 0.0;
+    while (icross <= ncross) {
+        double cross = 1.0;
+        while (cross > 0 && length < lmax) {  // at most lmax / h steps in all
+            double pre = pos[face];
+            pm_next(f, pos[0], pos[1], pos[2], h, status);
+            cross = (pre - init) * (pos[face] - init);
+            length += h;
+        }
+        if (length < lmax) {
+            xo[row + icross] = pos[0];
+            yo[row + icross] = pos[1];
+            zo[row + icross] = pos[2];
+            ++icross;
+        } else {
+            break;
+        }
+    }
+    found[i] = icross - 1;
+}
+
+cudaError_t launch_poincare(const DevField& f, int n, const double* seeds, int face, double h, double lmax,
+                            int ncross, double* xo, double* yo, double* zo, int* found, int* status,
+                            cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    poincare_kernel<<<(n + 127) / 128, 128, 0, s>>>(f, n, seeds, face, h, lmax, ncross, xo, yo, zo, found,
+                                                    status);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- host launchers
 cudaError_t launch_bc(const DevField& f, int n, double* st, int* iescape, cudaStream_t s)
 {

@@ -66,6 +66,16 @@ __host__ __device__ __forceinline__ uint32_t pack_offset(int l, int n, int k)
     return base + (uint32_t)(h * ka + a) * kStageBytes + tc::sw128_offset(128, n & 127, k & 63);
 }
 
+// SiLU of two values given as h = z / 2: h + h tanh(h), in BF16 pairs.
+__device__ __forceinline__ uint32_t silu_half_bf16x2(float h0, float h1)
+{
+    const uint32_t h = pack_bf16(h0, h1);
+    uint32_t t, r;
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(h));
+    asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(r) : "r"(h), "r"(t));
+    return r;
+}
+
 // Shared state of the block's tensor-core pipeline.
 struct Pipe {
     unsigned char* a[kTiles];        // activation tiles (A operands)
@@ -74,6 +84,7 @@ struct Pipe {
     uint32_t tmem;
     int* abort;
     const float* bias;               // shared copy: 4 x 256 hidden biases then 6 output biases
+    const float* hbias;              // halves of the 4 x 256 hidden biases
     const int* freq;
     // thread 0 only: chunk counters (monotonic) and layer-completion count
     uint32_t next_load, next_use, ndone;
@@ -178,17 +189,27 @@ __device__ __noinline__ void field_block(const Model& md, Pipe& pp, const uint64
             return;
         }
         if (l < kLayers - 1) {
-            const float* bias = pp.bias + l * kHid;
+            // SiLU(z) = h + h tanh(h), h = z / 2 = acc / 2 + bias / 2, in packed
+            // BF16 pairs (one tanh per two values); the result is already the
+            // next layer's BF16 input
+            const float4* hb4 = reinterpret_cast<const float4*>(pp.hbias + l * kHid);
+            const uint32_t rbase = (uint32_t)(row >> 3) * 1024u + (uint32_t)(row & 7) * 128u;
+            const uint32_t rx = (uint32_t)(row & 7);
 #pragma unroll 1
             for (int c0 = 0; c0 < kHid; c0 += 16) {
                 float v[16];
                 tc::tmem_ld16(tcol + (uint32_t)c0, v);
                 uint32_t pk[8];
 #pragma unroll
-                for (int q = 0; q < 8; q++)
-                    pk[q] = pack_bf16(silu(v[2 * q] + bias[c0 + 2 * q]), silu(v[2 * q + 1] + bias[c0 + 2 * q + 1]));
-                *reinterpret_cast<uint4*>(arow + tc::sw128_offset(128, row, c0)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                *reinterpret_cast<uint4*>(arow + tc::sw128_offset(128, row, c0 + 8)) =
+                for (int q = 0; q < 4; q++) {
+                    const float4 hb = hb4[(c0 >> 2) + q];
+                    pk[2 * q] = silu_half_bf16x2(fmaf(0.5f, v[4 * q], hb.x), fmaf(0.5f, v[4 * q + 1], hb.y));
+                    pk[2 * q + 1] = silu_half_bf16x2(fmaf(0.5f, v[4 * q + 2], hb.z), fmaf(0.5f, v[4 * q + 3], hb.w));
+                }
+                // 128-byte-swizzled row chunk positions of columns c0 and c0 + 8
+                const uint32_t atom = (uint32_t)(c0 >> 6) * 16384u, ch = (uint32_t)((c0 >> 3) & 7);
+                *reinterpret_cast<uint4*>(arow + atom + rbase + ((ch ^ rx) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                *reinterpret_cast<uint4*>(arow + atom + rbase + (((ch + 1) ^ rx) << 4)) =
                     make_uint4(pk[4], pk[5], pk[6], pk[7]);
             }
             tc::fence_async_smem();
@@ -212,6 +233,7 @@ __device__ __noinline__ void field_block(const Model& md, Pipe& pp, const uint64
 // mbarriers, tensor memory, and the first chunks in flight.
 struct SmemStatic {
     float bias[kLayers * kHid];
+    __align__(16) float hbias[(kLayers - 1) * kHid];
     int freq[3 * kFeat];
     uint64_t bars[2 * kStages + 1];
     uint32_t tmem_slot;
@@ -225,7 +247,10 @@ __device__ void pipe_setup(Pipe& pp, SmemStatic& st, unsigned char* dyn, const M
     unsigned char* base = dyn + ((1024u - (raw & 1023u)) & 1023u);
     for (int t = 0; t < kTiles; t++) pp.a[t] = base + t * kABytes;
     pp.stage0 = tc::smem_addr(base + kTiles * kABytes);
-    for (int k = tid; k < (kLayers - 1) * kHid; k += blockDim.x) st.bias[k] = md.b[k / kHid][k % kHid];
+    for (int k = tid; k < (kLayers - 1) * kHid; k += blockDim.x) {
+        st.bias[k] = md.b[k / kHid][k % kHid];
+        st.hbias[k] = 0.5f * st.bias[k];
+    }
     if (tid < kOut) st.bias[(kLayers - 1) * kHid + tid] = md.b[kLayers - 1][tid];
     for (int k = tid; k < 3 * kFeat; k += blockDim.x) st.freq[k] = md.freq[k];
     pp.full = tc::smem_addr(&st.bars[0]);
@@ -233,6 +258,7 @@ __device__ void pipe_setup(Pipe& pp, SmemStatic& st, unsigned char* dyn, const M
     pp.done = tc::smem_addr(&st.bars[2 * kStages]);
     pp.abort = &st.abort;
     pp.bias = st.bias;
+    pp.hbias = st.hbias;
     pp.freq = st.freq;
     pp.next_load = pp.next_use = pp.ndone = 0;
     if (tid == 0) {

@@ -1,7 +1,7 @@
 #!/usr/bin/env bash
 # Links the reference's own program (main.c and every module that is not on
 # the tracking hot path) against libtpgpu.so instead of tracking.o,
-# emfields.o, interpolation.o, force_free.o and wlcs.o.
+# emfields.o, interpolation.o, force_free.o, wlcs.o and poincare_map.o.
 #
 #   REF      reference tree (default: $TP_REFERENCE_DIR)
 #   CC       the reference's compiler (mpicc on a cluster)
@@ -27,7 +27,7 @@ LIBDIR="$HERE/_build"
 mkdir -p "$OUT/obj"
 FLAGS=(-O2 -fopenmp -fcommon -std=gnu99 -w -include stdbool.h -I"$REF/include" ${CFLAGS:-})
 KEEP=(main test_particle domain diagnostics particle_info data_io quick_sort bessel
-      poincare_map magnetic_field electric_field velocity_field)
+      magnetic_field electric_field velocity_field)
 for s in "${KEEP[@]}"; do
   "$CC" "${FLAGS[@]}" -c "$REF/src/$s.c" -o "$OUT/obj/$s.o"
 done

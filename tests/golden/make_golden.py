@@ -254,11 +254,36 @@ def source_digest():
     return h.hexdigest()
 
 
+def poincare_fixture(lib, sc):
+    """RK4 field-line steps of the reference (next_location,
+    src/poincare_map.c:243-290) from seeds in the gridded scenarios, including
+    steps that leave the box (periodic wrap of the stage points)."""
+    rng = np.random.default_rng(8)
+    out = {}
+    for name in ("mhd", "pic", "pic_off"):
+        keep = ref_setup(lib, sc[name])
+        d = sc[name]["dom"]
+        lo = np.array([d.xmin, d.ymin, d.zmin])
+        hi = np.array([d.xmax, d.ymax, d.zmax])
+        seeds = lo + rng.uniform(0, 1, size=(32, 3)) * (hi - lo)
+        step = 0.02 * float(np.min(hi - lo))
+        traj = np.zeros((32, 40, 3))
+        lib.refh_next_location(C.c_int(32), p(seeds), C.c_double(step), C.c_int(40), p(traj))
+        out[name + "_seeds"] = seeds
+        out[name + "_step"] = step
+        out[name + "_traj"] = traj
+        del keep
+    np.savez_compressed(os.path.join(HERE, "poincare.npz"), **out)
+
+
 def main():
     if po.build_ref() is None:
         print("reference tree absent; nothing generated")
         return 1
     lib = ref_lib()
+    if "--poincare" in sys.argv:  # this fixture alone
+        poincare_fixture(lib, scenarios())
+        return 0
     rng = np.random.default_rng(7)
     sc = scenarios()
     meta = {"reference_sources_sha256": source_digest(), "fixtures": {}}
@@ -387,6 +412,9 @@ def main():
                         y0=np.array([j[1] for j in jobs]), h0=np.array([j[3] for j in jobs]),
                         out=np.array(outs))
     del lo
+
+    # 9. Poincare map field-line steps
+    poincare_fixture(lib, sc)
 
     meta["fixtures"] = sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))
     with open(os.path.join(HERE, "golden_meta.json"), "w") as f:

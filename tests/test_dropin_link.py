@@ -1,5 +1,5 @@
 """The reference's own program links against libtpgpu.so in place of its
-tracking, emfields, interpolation, force_free and wlcs objects
+tracking, emfields, interpolation, force_free, wlcs and poincare_map objects
 (test_particle_gb300/link_reference.sh).  Needs the reference tree (read only)
 and a compiler; linking needs no GPU."""
 import os
@@ -36,8 +36,8 @@ def test_reference_program_links_against_library(tmp_path):
             exported.add(parts[2])
     # every hot-path function the reference's program calls comes from the library
     for name in ("particle_tracking_hybrid", "set_variables_tracking", "set_ptl_params_tracking",
-                 "set_variables_emfields", "get_emf", "get_magnetic_field", "getemf_ff",
+                 "set_variables_emfields", "get_emf", "getemf_ff",
                  "getemf_wlcs", "get_trilinar_parameters", "get_param_ff", "read_wlcs",
-                 "free_config", "adjust_dt_normI", "get_tracking_time_interval"):
+                 "free_config", "adjust_dt_normI", "get_tracking_time_interval", "poincare_map"):
         assert name in need, name
     assert need <= exported, sorted(need - exported)

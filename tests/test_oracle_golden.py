@@ -108,3 +108,40 @@ def test_bs_bitexact():
     for i in range(len(bs["y0"])):
         o = po.bs_integrate(f, bs["y0"][i], 0.0, float(bs["h0"][i]), bs["out"].shape[1])
         assert np.array_equal(o, bs["out"][i], equal_nan=True)
+
+
+@pytest.mark.parametrize("name", ["mhd", "pic", "pic_off"])
+def test_poincare_rk4_steps_bitexact(name):
+    """The field-line RK4 step (src/poincare_map.c:243-290) against the
+    reference's next_location, 40 steps from 32 seeds, wrap included."""
+    pc = load("poincare")
+    f = mg.field_from(SC[name])
+    got = po.next_location_steps(f, pc[name + "_seeds"], float(pc[name + "_step"]), 40)
+    assert np.array_equal(got, pc[name + "_traj"])
+
+
+def test_poincare_crossings_follow_the_steps():
+    """The crossing loop (src/poincare_map.c:158-181): every recorded point is
+    the first step after a sign change of pos[face] - seed[face], found by
+    replaying the RK4 steps; unfilled entries keep the fill value 2 * max."""
+    f = mg.field_from(SC["pic"])
+    d = SC["pic"]["dom"]
+    rng = np.random.default_rng(4)
+    seeds = np.array([d.xmin, d.ymin, d.zmin]) + rng.uniform(0, 1, size=(6, 3)) * \
+        np.array([d.xmax - d.xmin, d.ymax - d.ymin, d.zmax - d.zmin])
+    step, lmax, ncross, face = 0.05, 60.0, 5, 1
+    xo, yo, zo, found = po.poincare(f, seeds, face, step, lmax, ncross)
+    nsteps = int(np.ceil(lmax / step)) + 1
+    for i in range(len(seeds)):
+        traj = po.next_location_steps(f, seeds[i], step, nsteps)[0]
+        init = seeds[i, face]
+        pre = np.concatenate([[seeds[i, face]], traj[:-1, face]])
+        hits = np.nonzero((pre - init) * (traj[:, face] - init) <= 0)[0]
+        # the loop tests cross > 0 after each step, with the length bound
+        length = step * (hits + 1)
+        hits = hits[length < lmax][:ncross]
+        assert found[i] == len(hits)
+        assert np.array_equal(xo[i, 1:1 + len(hits)], traj[hits, 0])
+        assert np.array_equal(zo[i, 1:1 + len(hits)], traj[hits, 2])
+        assert np.all(yo[i, 1 + len(hits):] == 2 * d.ymax)
+        assert xo[i, 0] == seeds[i, 0]
