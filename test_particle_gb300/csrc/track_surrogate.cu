@@ -90,50 +90,65 @@ struct Pipe {
     uint32_t next_load, next_use, ndone;
 };
 
-__device__ __forceinline__ void issue_load(Pipe& pp, const unsigned char* wpack)
+// First chunk of each layer in the per-evaluation sequence (and the end).
+__host__ __device__ constexpr int layer_first_chunk(int l) { return l == 0 ? 0 : l < 5 ? 4 + 8 * (l - 1) : 32; }
+
+// Thread 0: the bulk copy of chunk c into its ring stage, once the MMAs that
+// read the stage's previous chunk have completed; false on a timed-out wait.
+__device__ __forceinline__ bool issue_load(uint32_t c, uint32_t full, uint32_t empty, uint32_t stage0,
+                                           const unsigned char* wpack)
 {
-    const uint32_t c = pp.next_load;
     const uint32_t s = c % kStages, use = c / kStages;
-    if (use > 0 && !tc::mbar_wait(pp.empty + 8 * s, (use - 1) & 1, kWaitLimit)) {
-        *pp.abort = 1;
-        return;
-    }
+    if (use > 0 && !tc::mbar_wait(empty + 8 * s, (use - 1) & 1, kWaitLimit)) return false;
     const Chunk ch = chunk_of((int)(c % kChunks));
-    tc::mbar_expect_tx(pp.full + 8 * s, ch.bytes);
-    tc::bulk_g2s(pp.stage0 + s * kStageBytes, wpack + ch.offset, ch.bytes, pp.full + 8 * s);
-    pp.next_load = c + 1;
+    tc::mbar_expect_tx(full + 8 * s, ch.bytes);
+    tc::bulk_g2s(stage0 + s * kStageBytes, wpack + ch.offset, ch.bytes, full + 8 * s);
+    return true;
 }
 
 // Thread 0: the MMAs of one layer (its chunks in sequence), refilling the
-// ring one chunk behind, then a commit to the layer barrier.
-__device__ void issue_layer(Pipe& pp, const unsigned char* wpack, int layer)
+// ring one chunk behind, then a commit to the layer barrier.  The ring state
+// lives in registers here; descriptors are built once and advanced by adding
+// to their start-address field (16-byte units).
+__device__ __noinline__ void issue_layer(Pipe& pp, const unsigned char* wpack, int layer)
 {
     const uint32_t idesc = tc::idesc_bf16_f32(128, layer == kLayers - 1 ? 16 : 128);
-    for (;;) {
-        const uint32_t c = pp.next_use;
-        const Chunk ch = chunk_of((int)(c % kChunks));
-        if (ch.layer != layer || *pp.abort) break;
+    const uint32_t full = pp.full, empty = pp.empty, stage0 = pp.stage0, tmem = pp.tmem;
+    uint64_t adesc[kTiles];
+#pragma unroll
+    for (int t = 0; t < kTiles; t++) adesc[t] = tc::desc_sw128(tc::smem_addr(pp.a[t]));
+    uint32_t next_use = pp.next_use, next_load = pp.next_load;
+    const uint32_t base = next_use - (next_use % kChunks);
+    const uint32_t c_end = base + (uint32_t)layer_first_chunk(layer + 1);
+    bool ok = !*pp.abort;
+    for (uint32_t c = next_use; ok && c < c_end; c++) {
         const uint32_t s = c % kStages, use = c / kStages;
-        if (!tc::mbar_wait(pp.full + 8 * s, use & 1, kWaitLimit)) {
-            *pp.abort = 1;
+        if (!tc::mbar_wait(full + 8 * s, use & 1, kWaitLimit)) {
+            ok = false;
             break;
         }
         tc::tc_fence_after();
-        const uint32_t b0 = pp.stage0 + s * kStageBytes;
+        const Chunk ch = chunk_of((int)(c % kChunks));
+        const uint64_t bdesc = tc::desc_sw128(stage0 + s * kStageBytes);
 #pragma unroll
         for (int t = 0; t < kTiles; t++) {
-            const uint32_t a0 = tc::smem_addr(pp.a[t]) + (uint32_t)ch.katom * 128u * 128u;
-            const uint32_t d = pp.tmem + (uint32_t)(t * 256 + ch.half * 128);
+            const uint64_t a = adesc[t] + (uint64_t)(ch.katom * (128 * 128 / 16));
+            const uint32_t d = tmem + (uint32_t)(t * 256 + ch.half * 128);
 #pragma unroll
             for (int kk = 0; kk < 4; kk++)
-                tc::mma_bf16(d, tc::desc_sw128(a0 + kk * 32), tc::desc_sw128(b0 + kk * 32), idesc,
-                             (ch.katom | kk) != 0);
+                tc::mma_bf16(d, a + 2 * kk, bdesc + 2 * kk, idesc, (ch.katom | kk) != 0);
         }
-        tc::mma_commit(pp.empty + 8 * s);
-        pp.next_use = c + 1;
+        tc::mma_commit(empty + 8 * s);
+        next_use = c + 1;
         // keep kStages - 1 chunks in flight: refill the stage the previous chunk used
-        while (pp.next_load < pp.next_use + kStages - 1 && !*pp.abort) issue_load(pp, wpack);
+        while (ok && next_load < next_use + kStages - 1) {
+            ok = issue_load(next_load, full, empty, stage0, wpack);
+            if (ok) next_load++;
+        }
     }
+    pp.next_use = next_use;
+    pp.next_load = next_load;
+    if (!ok) *pp.abort = 1;
     tc::mma_commit(pp.done);
 }
 
@@ -279,7 +294,8 @@ __device__ void pipe_setup(Pipe& pp, SmemStatic& st, unsigned char* dyn, const M
     tc::tc_fence_after();
     pp.tmem = st.tmem_slot;
     if (tid == 0)
-        while (pp.next_load < (uint32_t)(kStages - 1)) issue_load(pp, md.wpack);
+        for (; pp.next_load < (uint32_t)(kStages - 1); pp.next_load++)
+            issue_load(pp.next_load, pp.full, pp.empty, pp.stage0, md.wpack);
 }
 
 // Waits (bounded) for the copies still in flight, then frees tensor memory.
