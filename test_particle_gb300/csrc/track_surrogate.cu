@@ -40,15 +40,17 @@ struct Chunk {
     uint32_t bytes, offset;
 };
 
+// The two output halves of a k-atom are consecutive, so that they land in
+// adjacent ring stages and one N = 256 MMA reads both.
 __host__ __device__ __forceinline__ Chunk chunk_of(int j)
 {
     Chunk c;
     if (j < 4) {
-        c.layer = 0; c.half = j >> 1; c.katom = j & 1;
+        c.layer = 0; c.half = j & 1; c.katom = j >> 1;
         c.bytes = kStageBytes; c.offset = (uint32_t)j * kStageBytes;
     } else if (j < 28) {
         const int jj = (j - 4) & 7;
-        c.layer = 1 + (j - 4) / 8; c.half = jj >> 2; c.katom = jj & 3;
+        c.layer = 1 + (j - 4) / 8; c.half = jj & 1; c.katom = jj >> 1;
         c.bytes = kStageBytes; c.offset = 65536u + (uint32_t)(j - 4) * kStageBytes;
     } else {
         c.layer = 4; c.half = 0; c.katom = j - 28;
@@ -61,9 +63,9 @@ __host__ __device__ __forceinline__ Chunk chunk_of(int j)
 __host__ __device__ __forceinline__ uint32_t pack_offset(int l, int n, int k)
 {
     if (l == kLayers - 1) return 458752u + (uint32_t)(k >> 6) * 2048u + tc::sw128_offset(16, n, k & 63);
-    const int ka = layer_in(l) / 64, h = n >> 7, a = k >> 6;
+    const int h = n >> 7, a = k >> 6;
     const uint32_t base = l == 0 ? 0u : 65536u + (uint32_t)(l - 1) * 131072u;
-    return base + (uint32_t)(h * ka + a) * kStageBytes + tc::sw128_offset(128, n & 127, k & 63);
+    return base + (uint32_t)(2 * a + h) * kStageBytes + tc::sw128_offset(128, n & 127, k & 63);
 }
 
 // SiLU of two values given as h = z / 2: h + h tanh(h), in BF16 pairs.
@@ -106,13 +108,16 @@ __device__ __forceinline__ bool issue_load(uint32_t c, uint32_t full, uint32_t e
     return true;
 }
 
-// Thread 0: the MMAs of one layer (its chunks in sequence), refilling the
-// ring one chunk behind, then a commit to the layer barrier.  The ring state
-// lives in registers here; descriptors are built once and advanced by adding
-// to their start-address field (16-byte units).
+// Thread 0: the MMAs of one layer.  Hidden layers go by k-atom: its two
+// output halves sit in adjacent stages (a stage pair), and each MMA covers
+// N = 256 outputs; after issuing a pair it refills the other pair, whose MMAs
+// were issued one step earlier.  The output layer (N = 16) goes chunk by
+// chunk.  Ring state in registers; descriptors built once and advanced by
+// adding to their start-address field (16-byte units).
 __device__ __noinline__ void issue_layer(Pipe& pp, const unsigned char* wpack, int layer)
 {
-    const uint32_t idesc = tc::idesc_bf16_f32(128, layer == kLayers - 1 ? 16 : 128);
+    const bool last = layer == kLayers - 1;
+    const uint32_t idesc = tc::idesc_bf16_f32(128, last ? 16 : 256);
     const uint32_t full = pp.full, empty = pp.empty, stage0 = pp.stage0, tmem = pp.tmem;
     uint64_t adesc[kTiles];
 #pragma unroll
@@ -120,28 +125,28 @@ __device__ __noinline__ void issue_layer(Pipe& pp, const unsigned char* wpack, i
     uint32_t next_use = pp.next_use, next_load = pp.next_load;
     const uint32_t base = next_use - (next_use % kChunks);
     const uint32_t c_end = base + (uint32_t)layer_first_chunk(layer + 1);
+    const uint32_t width = last ? 1u : 2u;  // chunks per MMA group
     bool ok = !*pp.abort;
-    for (uint32_t c = next_use; ok && c < c_end; c++) {
-        const uint32_t s = c % kStages, use = c / kStages;
-        if (!tc::mbar_wait(full + 8 * s, use & 1, kWaitLimit)) {
-            ok = false;
-            break;
-        }
+    for (uint32_t c = next_use; ok && c < c_end; c += width) {
+        const uint32_t s = c % kStages;
+        for (uint32_t w = 0; w < width && ok; w++)
+            ok = tc::mbar_wait(full + 8 * ((c + w) % kStages), ((c + w) / kStages) & 1, kWaitLimit);
+        if (!ok) break;
         tc::tc_fence_after();
         const Chunk ch = chunk_of((int)(c % kChunks));
         const uint64_t bdesc = tc::desc_sw128(stage0 + s * kStageBytes);
 #pragma unroll
         for (int t = 0; t < kTiles; t++) {
             const uint64_t a = adesc[t] + (uint64_t)(ch.katom * (128 * 128 / 16));
-            const uint32_t d = tmem + (uint32_t)(t * 256 + ch.half * 128);
+            const uint32_t d = tmem + (uint32_t)(t * 256);
 #pragma unroll
             for (int kk = 0; kk < 4; kk++)
                 tc::mma_bf16(d, a + 2 * kk, bdesc + 2 * kk, idesc, (ch.katom | kk) != 0);
         }
-        tc::mma_commit(empty + 8 * s);
-        next_use = c + 1;
-        // keep kStages - 1 chunks in flight: refill the stage the previous chunk used
-        while (ok && next_load < next_use + kStages - 1) {
+        for (uint32_t w = 0; w < width; w++) tc::mma_commit(empty + 8 * ((c + w) % kStages));
+        next_use = c + width;
+        // refill up to one stage pair ahead of the next group
+        while (ok && next_load < next_use + kStages - width) {
             ok = issue_load(next_load, full, empty, stage0, wpack);
             if (ok) next_load++;
         }
