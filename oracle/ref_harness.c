@@ -252,6 +252,32 @@ void refh_track_fixed(int nptl, double dt, int nbins, int nt_out,
     free(etot);
 }
 
+/* The same run with trajectory diagnostics (src/tracking.c:90-190 with
+ * traj_diagnose = 1): ptl_time holds each particle's records at
+ * ntraj_accum[i-1] (the caller stores the initial state there, as
+ * src/diagnostics.c:541-551 does); a record is added every nsteps_output steps. */
+void refh_track_traj(int nptl, double dt, int nbins, int nt_out, int nsteps_output,
+        int *ntraj_accum, particles *ptl_init, particles *ptl, int *nsteps_ptl,
+        particles *ptl_time)
+{
+    int nth = omp_get_max_threads();
+    size_t per = (size_t)nbins * nt_out;
+    double *ep = (double *)calloc((size_t)(nth + 1) * per, sizeof(double));
+    double *eep = (double *)calloc((size_t)(nth + 1) * per, sizeof(double));
+    double *etot = (double *)calloc(per, sizeof(double));
+    double *es = (double *)calloc(per, sizeof(double));
+    double *ee = (double *)calloc(per, sizeof(double));
+    particle_tracking_fixed_time_step(0, nptl, dt, nbins, nt_out, 1, nsteps_output, 1.0,
+            ntraj_accum, ptl_init, nsteps_ptl, ptl, (double (*)[nbins])es,
+            (double (*)[nbins])etot, (double (*)[nbins])ee,
+            (double (*)[nbins * nt_out])ep, (double (*)[nbins * nt_out])eep, ptl_time);
+    free(ep);
+    free(eep);
+    free(etot);
+    free(es);
+    free(ee);
+}
+
 /* Bulirsch-Stoer: nsteps accepted steps of one particle through the
  * reference's step() without dense output.  step() keeps its controller in
  * function-static variables, so a caller pins one particle per fresh process.
@@ -299,4 +325,25 @@ void refh_next_location(int n, const double *xyz, double step, int nsteps, doubl
             o[0] = x; o[1] = y; o[2] = z;
         }
     }
+}
+
+/* ---------------------------------------------------------------- field files
+ * The reference's binary readers for one time frame of float data
+ * (src/magnetic_field.c:442-534, src/electric_field.c:257-349): reads
+ * <path>{bx,by,bz}_<ct>.gda scaled by B0 and {ex,ey,ez} by E0 into its own
+ * arrays, copied out as nx*ny*nz {x,y,z} float records. */
+void refh_read_pic_binary(grids *sgrid, domain *sdomain, char *path, int ct, double b0, double e0,
+        float *out_b, float *out_e)
+{
+    size_t n = (size_t)sgrid->nx * sgrid->ny * sgrid->nz;
+    set_variables_bfield(sgrid, sdomain, b0, 0, sizeof(float));
+    initialize_bfield();
+    read_bfields_binary(path, ct, sizeof(float));
+    memcpy(out_b, magc_float, sizeof(float) * 3 * n);
+    free_bfield();
+    set_variables_efield(sgrid, sdomain, e0, 0, sizeof(float));
+    initialize_efield();
+    read_efields_binary(path, ct, sizeof(float));
+    memcpy(out_e, efc_float, sizeof(float) * 3 * n);
+    free_efield();
 }

@@ -254,6 +254,65 @@ def source_digest():
     return h.hexdigest()
 
 
+def traj_fixture(lib, sc):
+    """Trajectory diagnostics (particle_tracking_fixed_time_step with
+    traj_diagnose = 1): records every nsteps_output steps into ptl_time at
+    each particle's offset, the initial state first (src/diagnostics.c:541-551,
+    src/tracking.c:436-447)."""
+    rng = np.random.default_rng(31)
+    out = {}
+    for name, n, dt, steps, every in (("pic", 24, 0.05, 160, 16), ("test", 16, 0.05, 120, 10)):
+        d = po.Domain.from_buffer_copy(sc[name]["dom"])
+        d.tmax = steps * dt + 0.5 * dt
+        s = dict(sc[name])
+        s["dom"] = d
+        keep = ref_setup(lib, s, 0)
+        lib.refh_set_spectrum(C.c_int(20), C.c_double(1e-3), C.c_double(1e1))
+        p0 = particles_for(s, rng, n)
+        pp = p0.copy()
+        nst = np.zeros(n, dtype=np.int32)
+        npts = np.full(n, steps // every + 1, dtype=np.int32)  # every particle runs all steps
+        acc = np.cumsum(npts).astype(np.int32)
+        ptl_time = np.zeros(int(acc[-1]), dtype=PD)
+        off = np.concatenate([[0], acc[:-1]])
+        ptl_time[off] = p0
+        lib.refh_track_traj(C.c_int(n), C.c_double(dt), C.c_int(20), C.c_int(2), C.c_int(every), p(acc),
+                            p(p0.copy()), p(pp), p(nst), p(ptl_time))
+        out[name + "_ptl0"] = p0
+        out[name + "_ptl"] = pp
+        out[name + "_acc"] = acc
+        out[name + "_ptl_time"] = ptl_time
+        out[name + "_meta"] = np.array([dt, steps, every, d.tmax])
+        del keep
+    np.savez_compressed(os.path.join(HERE, "traj.npz"), **out)
+
+
+def fields_fixture(lib):
+    """The reference's binary field readers (read_bfields_binary /
+    read_efields_binary, float data, one frame): random .gda component files
+    and the scaled {x,y,z} records the reference builds from them."""
+    import tempfile
+    rng = np.random.default_rng(41)
+    nx, ny, nz, ct = 12, 10, 7, 3
+    b0, e0 = 0.37, 1.9e-3
+    comps = rng.normal(0, 1, size=(6, nz * ny * nx)).astype(np.float32)
+    comps *= np.float32(10.0) ** rng.integers(-3, 3, size=comps.shape).astype(np.float32)
+    g = po.Grids()
+    g.nx, g.ny, g.nz, g.nt = nx, ny, nz, 1
+    g.dx = g.dy = g.dz = 1.0
+    d = po.Domain()
+    d.xmax, d.ymax, d.zmax = nx - 1.0, ny - 1.0, nz - 1.0
+    with tempfile.TemporaryDirectory() as tmp:
+        for c, name in enumerate(("bx", "by", "bz", "ex", "ey", "ez")):
+            comps[c].tofile(os.path.join(tmp, "%s_%d.gda" % (name, ct)))
+        out_b = np.zeros(3 * nx * ny * nz, dtype=np.float32)
+        out_e = np.zeros(3 * nx * ny * nz, dtype=np.float32)
+        lib.refh_read_pic_binary(C.byref(g), C.byref(d), (tmp + "/").encode(), C.c_int(ct), C.c_double(b0),
+                                 C.c_double(e0), p(out_b), p(out_e))
+    np.savez_compressed(os.path.join(HERE, "fields.npz"), comps=comps, dims=np.array([nx, ny, nz, ct]),
+                        scale=np.array([b0, e0]), records_b=out_b, records_e=out_e)
+
+
 def poincare_fixture(lib, sc):
     """RK4 field-line steps of the reference (next_location,
     src/poincare_map.c:243-290) from seeds in the gridded scenarios, including
@@ -283,6 +342,12 @@ def main():
     lib = ref_lib()
     if "--poincare" in sys.argv:  # this fixture alone
         poincare_fixture(lib, scenarios())
+        return 0
+    if "--traj" in sys.argv:  # this fixture alone
+        traj_fixture(lib, scenarios())
+        return 0
+    if "--fields" in sys.argv:  # this fixture alone
+        fields_fixture(lib)
         return 0
     rng = np.random.default_rng(7)
     sc = scenarios()
@@ -415,6 +480,10 @@ def main():
 
     # 9. Poincare map field-line steps
     poincare_fixture(lib, sc)
+    # 10. trajectory diagnostics
+    traj_fixture(lib, sc)
+    # 11. binary field files
+    fields_fixture(lib)
 
     meta["fixtures"] = sorted(f for f in os.listdir(HERE) if f.endswith(".npz"))
     with open(os.path.join(HERE, "golden_meta.json"), "w") as f:
