@@ -293,6 +293,18 @@ int tp_poincare_trace(int n, const double *seeds, int face, double step, double 
 void tp_poincare_save(int mpi_rank, int mpi_size, int npoints_total, int ncross, int nshift,
                       int npoints, const double *xpos, const double *ypos, const double *zpos);
 
+/* PIC-style fields (system type 4) of the current grid from the reference's
+ * binary files <filepath>{bx,by,bz,ex,ey,ez}_<ct>.gda (nx*ny*nz FP32 each,
+ * x fastest), scaled by B0 and E0 as read_bfields_binary /
+ * read_efields_binary do (src/magnetic_field.c:442-534,
+ * src/electric_field.c:257-349, one time frame), straight into device memory;
+ * the host arrays magc_float / efc_float are not filled.  tp_mark_fields_dirty
+ * or tp_release_device_fields return to the host arrays. */
+int tp_read_pic_fields_binary(const char *filepath, int ct);
+/* Copies device-resident PIC-style fields (tp_read_pic_fields_binary,
+ * tp_synth_pic_fields) to host arrays of nx*ny*nz {x,y,z} float records. */
+int tp_fetch_device_fields(float *host_e, float *host_b);
+
 /* One call, host buffers in and out (reuses a cached session). */
 int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,
                   const particles *ptl_init, particles *ptl, int *nsteps_ptl,

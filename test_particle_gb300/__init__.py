@@ -381,3 +381,21 @@ def poincare_trace(seeds, face, step, length_max, ncross):
                                   C.c_double(length_max), C.c_int(ncross), _ptr(xo), _ptr(yo),
                                   _ptr(zo), _ptr(found)), "poincare_trace")
     return xo, yo, zo, found
+
+
+def read_pic_fields_binary(filepath, ct):
+    """Load <filepath>{bx,by,bz,ex,ey,ez}_<ct>.gda into device memory
+    (tp_read_pic_fields_binary), scaled by the B0 / E0 set through
+    set_variables_bfield / set_variables_efield."""
+    check(lib().tp_read_pic_fields_binary(str(filepath).encode(), C.c_int(ct)), "read_pic_fields_binary")
+
+
+def fetch_device_fields():
+    """Host copies (E, B) of the device-resident PIC-style fields, n x 3 float32."""
+    L = lib()
+    g = Grids.in_dll(L, "simul_grid")
+    n = g.nx * g.ny * g.nz
+    he = np.zeros((n, 3), dtype=np.float32)
+    hb = np.zeros((n, 3), dtype=np.float32)
+    check(L.tp_fetch_device_fields(_ptr(he), _ptr(hb)), "fetch_device_fields")
+    return he, hb

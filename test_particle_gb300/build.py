@@ -35,6 +35,7 @@ UNITS = [
     ("noalloc.o", "noalloc.cu", []),
     ("tc_gemm.o", "tc_gemm.cu", []),
     ("poincare.o", "poincare.cu", []),
+    ("loaders.o", "loaders.cu", []),
 ]
 
 

@@ -145,3 +145,15 @@ def test_poincare_crossings_follow_the_steps():
         assert np.array_equal(zo[i, 1:1 + len(hits)], traj[hits, 2])
         assert np.all(yo[i, 1 + len(hits):] == 2 * d.ymax)
         assert xo[i, 0] == seeds[i, 0]
+
+
+def test_field_file_records_restated():
+    """The reference's binary readers store float(data * B0) with the product
+    in double (src/magnetic_field.c:458-474); the fixture made by them agrees
+    with that restatement bit for bit."""
+    f = load("fields")
+    c = f["comps"]
+    b0, e0 = f["scale"]
+    rb = (c[:3].T.astype(np.float64) * b0).astype(np.float32).ravel()
+    re_ = (c[3:].T.astype(np.float64) * e0).astype(np.float32).ravel()
+    assert np.array_equal(rb, f["records_b"]) and np.array_equal(re_, f["records_e"])
