@@ -300,6 +300,19 @@ def config_bench(name, args):
             info = sess.track(dt, max(1, st // 1000), cfg["nbins"], code)
             rates[label] = {"pushes_per_s": info.pushes / info.kernel_ms * 1e3, "steps": st,
                             "particles": n, "kernel_ms": info.kernel_ms}
+        if name == "surrogate":
+            # what the model gains: the exact sum's cost grows with the mode count, the model's does not
+            big = wl.kolmogorov_modes(4096, cfg["kmin"], cfg["kmax"], cfg["dB"], cfg["seed"] + 5, va=cfg["va"])
+            tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=big, mode_B0=cfg["B0"])
+            tp.set_spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
+            st = min(steps, 50)
+            tp.set_tmax(st * dt + 0.5 * dt)
+            sess.load(p0)
+            info = sess.track(dt, 1, cfg["nbins"], tp.PREC_MIXED)
+            rates["mixed_exact_4096_modes"] = {"pushes_per_s": info.pushes / info.kernel_ms * 1e3, "steps": st,
+                                               "particles": n, "kernel_ms": info.kernel_ms}
+            tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=cfg["B0"])
+            tp.set_spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
         out["rates"] = rates
         # accuracy of the fast path(s) against FP64 (or against the exact field for the surrogate)
         na, sa = args.acc_nptl, args.acc_steps

@@ -135,3 +135,34 @@ def test_tensor_core_inference_matches_fp64_forward():
     gemm = tp.mlp_eval(u)
     assert np.abs(got - gemm).max() < 2e-2 * scale
     assert tp.device_status() == 0
+
+
+def test_model_cost_does_not_grow_with_the_mode_count():
+    """What the learned field gains over the method without it: the exact
+    plane-wave sum costs in proportion to its modes, the model a fixed chain
+    of GEMMs; at 4096 modes tracking with the model is faster than with the
+    exact FP32 sum (an untrained model does the same work as a trained one)."""
+    modes = wl.kolmogorov_modes(4096, 1, 64, 1.0, 5, va=0.1)
+    dom = tp.Domain()
+    dom.xmax = dom.ymax = dom.zmax = 1.0
+    steps = 20
+    dt = wl.gyro_dt(0.7, 1.0)
+    dom.tmax = steps * dt + 0.5 * dt
+    tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=1.0)
+    tp.set_spectrum(200, 1e-3, 1e2)
+    amp = np.linalg.norm(modes["amp_b"], axis=1)
+    tp.mlp_init(modes["n"][np.argsort(-amp)[:64]], seed=3)
+    tp.mlp_set_output_norm(np.array([0, 0, 1, 0, 0, 0]), np.ones(6))
+    p0 = wl.shell_particles(65536, 0.7, (0, 0, 0), (1, 1, 1), 6)
+    s = tp.Session(len(p0))
+    ms = {}
+    for label, code in (("exact", tp.PREC_MIXED), ("model", tp.PREC_SURROGATE)):
+        best = None
+        for _ in range(2):  # the first run includes one-time set-up
+            s.load(p0)
+            info = s.track(dt, 1, 200, code)
+            best = info.kernel_ms if best is None else min(best, info.kernel_ms)
+        ms[label] = best
+    s.close()
+    assert ms["exact"] > 1.3 * ms["model"], ms
+    assert tp.device_status() == 0
