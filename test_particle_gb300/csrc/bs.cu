@@ -27,6 +27,9 @@ struct BsConst {
     int kmaxx;
     int k_targ0;
     double atol, rtol;
+    // host-computed powers of the step control: facmin[k] = STEPFAC3^(1/(2k+1))
+    // (the reference's pow(STEPFAC3, expo)) and expo[k] = 1/(2k+1)
+    double facmin[kImax], expo[kImax];
 };
 
 __constant__ BsConst c_bs;
@@ -112,6 +115,9 @@ __device__ __forceinline__ void midpoint(const DevField& f, int uform, double x,
     for (int i = 0; i < kNv; i++) yend[i] = 0.5 * (ym[i] + yn[i] + h * yend[i]);
 }
 
+__device__ __forceinline__ double sqr(double v) { return v * v; }
+__device__ __forceinline__ double sqr_int(int v) { return (double)v * (double)v; }
+
 struct Ctrl {
     bool first_step = true, last_step = false, reject = false, prev_reject = false;
 };
@@ -123,7 +129,7 @@ __device__ int bs_step(const DevField& f, int uform, int max_rejects, bool nan_r
                        double* y, double* dydx, double htry, double hnext_in, Ctrl& c,
                        double& hdid, double& hnext_out, int* status)
 {
-    const double STEPFAC1 = 0.65, STEPFAC2 = 0.94, STEPFAC3 = 0.02, STEPFAC4 = 4.0;
+    const double STEPFAC1 = 0.65, STEPFAC2 = 0.94, STEPFAC4 = 4.0;  // STEPFAC3 = 0.02: c_bs.facmin
     const double KFAC1 = 0.8, KFAC2 = 0.9;
     const int KMAXX = c_bs.kmaxx;
     double table[kImax][kNv];
@@ -162,7 +168,9 @@ __device__ int bs_step(const DevField& f, int uform, int max_rejects, bool nan_r
                 err = 0.0;
                 for (int i = 0; i < kNv; i++) {
                     scale = c_bs.atol + c_bs.rtol * fmax(fabs(ysav[i]), fabs(y[i]));
-                    err += pow((y[i] - table[0][i]) / scale, 2.0);
+                    // pow(q, 2.0) of the reference: the correctly rounded square, q * q
+                    const double q = (y[i] - table[0][i]) / scale;
+                    err += q * q;
                 }
                 err = sqrt(err / kNv);
                 if (nan_rejects && !(err == err)) {
@@ -173,8 +181,8 @@ __device__ int bs_step(const DevField& f, int uform, int max_rejects, bool nan_r
                     hnew = 0.25 * fabs(h);
                     break;
                 }
-                double expo = 1.0 / (2 * k + 1);
-                double facmin = pow(STEPFAC3, expo);
+                const double expo = c_bs.expo[k];
+                const double facmin = c_bs.facmin[k];
                 if (err == 0.0) {
                     fac = 1.0 / facmin;
                 } else {
@@ -186,8 +194,9 @@ __device__ int bs_step(const DevField& f, int uform, int max_rejects, bool nan_r
                 if ((c.first_step || c.last_step) && err <= 1.0) break;
                 if (k == k_targ - 1 && !c.prev_reject && !c.first_step && !c.last_step) {
                     if (err <= 1.0) break;
-                    else if (err > pow(c_bs.nseq[k_targ] * c_bs.nseq[k_targ + 1] /
-                                           (c_bs.nseq[0] * c_bs.nseq[0]), 2.0)) {
+                    // pow(integer ratio, 2.0) of the reference: an exact square
+                    else if (err > sqr_int(c_bs.nseq[k_targ] * c_bs.nseq[k_targ + 1] /
+                                           (c_bs.nseq[0] * c_bs.nseq[0]))) {
                         c.reject = true;
                         k_targ = k;
                         if (k_targ > 1 && work[k - 1] < KFAC1 * work[k]) k_targ--;
@@ -197,7 +206,7 @@ __device__ int bs_step(const DevField& f, int uform, int max_rejects, bool nan_r
                 }
                 if (k == k_targ) {
                     if (err <= 1.0) break;
-                    else if (err > pow((double)c_bs.nseq[k + 1] / c_bs.nseq[0], 2.0)) {
+                    else if (err > sqr((double)c_bs.nseq[k + 1] / c_bs.nseq[0])) {
                         c.reject = true;
                         if (k_targ > 1 && work[k - 1] < KFAC1 * work[k]) k_targ--;
                         hnew = hopt[k_targ];
@@ -296,94 +305,332 @@ __global__ void bs_steps_kernel(DevField f, BsArgs a)
     a.pstatus[i] = st;
 }
 
+// Diffusion sums and energy bin of one particle landing on frame `frame`.
+__device__ void frame_diagnostics(const DevField& f, const BsArgs& a, int frame, double x, double t0,
+                                  const double* y, const double* y0)
+{
+    double g = gamma_of(a.uform, y);
+    atomicAdd(&a.espect[frame * a.nbins + ebin(a.ebin_thr, a.nbins, g - 1.0)], 1u);
+    // diffusion coefficients at the frame, src/diagnostics.c:659-705
+    double tt = x * 2.0 - t0 * 2.0 + a.t_end / a.nt_out;
+    double d0 = y0[0] - y[0], d1 = y0[1] - y[1], d2 = y0[2] - y[2];
+    double g0 = gamma_of(a.uform, y0);
+    double u[3], u0[3];
+    for (int k = 0; k < 3; k++) {
+        u[k] = a.uform ? y[3 + k] : g * y[3 + k];
+        u0[k] = a.uform ? y0[3 + k] : g0 * y0[3 + k];
+    }
+    double du0 = u0[0] - u[0], du1 = u0[1] - u[1], du2 = u0[2] - u[2];
+    double e[6], e0[6];
+    emf64<TP_SYS_WLCS>(f, y[0], y[1], y[2], x, e, a.status);
+    emf64<TP_SYS_WLCS>(f, y0[0], y0[1], y0[2], t0, e0, a.status);
+    double mu = (e[0] * u[0] + e[1] * u[1] + e[2] * u[2]) /
+                (sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
+    double mu0 = (e0[0] * u0[0] + e0[1] * u0[1] + e0[2] * u0[2]) /
+                 (sqrt(e0[0] * e0[0] + e0[1] * e0[1] + e0[2] * e0[2]) * sqrt(u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]));
+    double th = acos(mu) * 180 / TP_PI, th0 = acos(mu0) * 180 / TP_PI;
+    double v[8];
+    v[1] = d0 * d0 / tt; v[2] = d1 * d1 / tt; v[3] = d2 * d2 / tt;
+    v[0] = v[1] + v[2] + v[3];
+    v[4] = (du0 * du0 + du1 * du1 + du2 * du2) / tt;
+    v[5] = (mu - mu0) * (mu - mu0) / tt;
+    v[6] = (th - th0) * (th - th0) / tt;
+    v[7] = (g - g0) * (g - g0) / tt;
+    double* slot = a.dframe + (size_t)(frame + 1) * 8;
+    for (int k = 0; k < 8; k++) atomicAdd(slot + k, v[k]);
+}
+
 // Production mode: every particle from its t to t_end; step sizes clipped to
 // land on the nt_out frame times t_end * (f+1) / nt_out, where the energy
 // spectrum and diffusion sums are taken.
+//
+// The stepper of bs_step restated as a state machine whose every turn makes
+// exactly one derivs call (a midpoint substep, the derivative at the end of
+// an accepted step, or the first derivative of a new particle): the lanes of
+// a warp sit at different points of their own steps, but all of them run the
+// field evaluation -- the bulk of the work -- together instead of one path at
+// a time.  The arithmetic and its order are those of bs_step.
 __global__ void __launch_bounds__(128) bs_track_kernel(DevField f, BsArgs a)
 {
-    for (;;) {
-        int i = atomicAdd(a.next, 1);
-        if (i >= a.n) break;
-        double y[kNv], dydx[kNv], y0[kNv];
-        for (int k = 0; k < kNv; k++) {
-            y[k] = a.y[kNv * i + k];
-            y0[k] = a.y0[kNv * i + k];
+    enum : int { P_INIT, P_MID, P_FINAL };
+    const double STEPFAC1 = 0.65, STEPFAC2 = 0.94, STEPFAC4 = 4.0;
+    const double KFAC1 = 0.8, KFAC2 = 0.9;
+    const int KMAXX = c_bs.kmaxx;
+    // particle
+    int i = atomicAdd(a.next, 1);
+    double y[kNv], dydx[kNv], y0[kNv];
+    double x = 0.0, t0 = 0.0, hnext = 0.0, tf = 0.0;
+    int st = 0, nacc = 0, frame = 0;
+    Ctrl c;
+    // step and attempt
+    double table[kImax][kNv], hopt[kImax], work[kImax], ysav[kNv];
+    double h = 0.0, hnew = 0.0, htry = 0.0, hprev = 0.0, err = 0.0;
+    int k_targ = 0, k = 0, nrej = 0;
+    bool forward = true, clip = false;
+    // midpoint
+    double ym[kNv], yn[kNv], hh = 0.0, xnew = 0.0;
+    int nn = 0;
+    int phase = P_INIT;
+    if (i < a.n) {
+        for (int q = 0; q < kNv; q++) {
+            y[q] = a.y[kNv * i + q];
+            y0[q] = a.y0[kNv * i + q];
         }
-        double x = a.t[i], hnext = a.h[i], hdid = 0.0;
-        const double t0 = x;
-        Ctrl c;
-        derivs(f, a.uform, x, y, dydx, a.status);
-        int st = 0, nacc = 0;
-        int frame = 0;
-        double tf = a.t_end * (frame + 1) / a.nt_out;
-        while (frame < a.nt_out && st == 0) {
-            if (nacc >= a.max_steps) {
+        x = a.t[i];
+        hnext = a.h[i];
+    }
+    // each turn: one derivs call per lane that still has a particle
+    while (i < a.n) {
+        // one call site, so that the lanes of a warp run it together
+        double yd[kNv], ye[kNv];
+        for (int q = 0; q < kNv; q++) ye[q] = phase == P_MID ? yn[q] : y[q];
+        const double xe = phase == P_MID ? xnew : phase == P_FINAL ? x + h : x;
+        derivs(f, a.uform, xe, ye, yd, a.status);
+
+        bool begin_step = false;   // set up the next step of this particle
+        bool finish = false;       // this particle is done (or failed)
+        if (phase == P_INIT) {
+            for (int q = 0; q < kNv; q++) dydx[q] = yd[q];
+            t0 = x;
+            c = Ctrl();
+            st = 0;
+            nacc = 0;
+            frame = 0;
+            tf = a.t_end * (frame + 1) / a.nt_out;
+            begin_step = true;
+        } else if (phase == P_MID) {
+            if (nn + 1 < c_bs.nseq[k]) {  // the next substep of the midpoint
+                const double h2 = 2.0 * hh;
+                for (int q = 0; q < kNv; q++) {
+                    double swap = ym[q] + h2 * yd[q];
+                    ym[q] = yn[q];
+                    yn[q] = swap;
+                }
+                xnew += hh;
+                nn++;
+                continue;
+            }
+            double yseq[kNv];
+            for (int q = 0; q < kNv; q++) yseq[q] = 0.5 * (ym[q] + yn[q] + hh * yd[q]);
+            // level k of the extrapolation (the loop body of bs_step)
+            int outcome = 0;  // 0: next level, 1: accept, 2: reject
+            if (k == 0) {
+                for (int q = 0; q < kNv; q++) y[q] = yseq[q];
+            } else {
+                for (int q = 0; q < kNv; q++) table[k - 1][q] = yseq[q];
+                for (int j = k - 1; j > 0; j--)
+                    for (int q = 0; q < kNv; q++)
+                        table[j - 1][q] = table[j][q] + c_bs.coeff[k][j] * (table[j][q] - table[j - 1][q]);
+                for (int q = 0; q < kNv; q++) y[q] = table[0][q] + c_bs.coeff[k][0] * (table[0][q] - y[q]);
+                err = 0.0;
+                for (int q = 0; q < kNv; q++) {
+                    double scale = c_bs.atol + c_bs.rtol * fmax(fabs(ysav[q]), fabs(y[q]));
+                    const double r = (y[q] - table[0][q]) / scale;
+                    err += r * r;
+                }
+                err = sqrt(err / kNv);
+                if (!(err == err)) {  // left the domain of the equations: retry a quarter step
+                    c.reject = true;
+                    hnew = 0.25 * fabs(h);
+                    outcome = 2;
+                } else {
+                    const double expo = c_bs.expo[k], facmin = c_bs.facmin[k];
+                    double fac;
+                    if (err == 0.0) {
+                        fac = 1.0 / facmin;
+                    } else {
+                        fac = STEPFAC2 / pow(err / STEPFAC1, expo);
+                        fac = fmax(facmin / STEPFAC4, fmin(1.0 / facmin, fac));
+                    }
+                    hopt[k] = fabs(h * fac);
+                    work[k] = c_bs.cost[k] / hopt[k];
+                    if ((c.first_step || c.last_step) && err <= 1.0) {
+                        outcome = 1;
+                    } else if (k == k_targ - 1 && !c.prev_reject && !c.first_step && !c.last_step &&
+                               (err <= 1.0 || err > sqr_int(c_bs.nseq[k_targ] * c_bs.nseq[k_targ + 1] /
+                                                            (c_bs.nseq[0] * c_bs.nseq[0])))) {
+                        if (err <= 1.0) {
+                            outcome = 1;
+                        } else {
+                            c.reject = true;
+                            k_targ = k;
+                            if (k_targ > 1 && work[k - 1] < KFAC1 * work[k]) k_targ--;
+                            hnew = hopt[k_targ];
+                            outcome = 2;
+                        }
+                    } else if (k == k_targ &&
+                               (err <= 1.0 || err > sqr((double)c_bs.nseq[k + 1] / c_bs.nseq[0]))) {
+                        if (err <= 1.0) {
+                            outcome = 1;
+                        } else {
+                            c.reject = true;
+                            if (k_targ > 1 && work[k - 1] < KFAC1 * work[k]) k_targ--;
+                            hnew = hopt[k_targ];
+                            outcome = 2;
+                        }
+                    } else if (k == k_targ + 1) {
+                        if (err > 1.0) {
+                            c.reject = true;
+                            if (k_targ > 1 && work[k_targ - 1] < KFAC1 * work[k_targ]) k_targ--;
+                            hnew = hopt[k_targ];
+                            outcome = 2;
+                        } else {
+                            outcome = 1;
+                        }
+                    }
+                }
+            }
+            if (outcome == 0) {  // the next level's midpoint
+                k++;
+                hh = h / c_bs.nseq[k];
+                for (int q = 0; q < kNv; q++) {
+                    ym[q] = ysav[q];
+                    yn[q] = ysav[q] + hh * dydx[q];
+                }
+                xnew = x + hh;
+                nn = 0;
+                continue;
+            }
+            if (outcome == 1) {  // accepted: the derivative at the end of the step
+                phase = P_FINAL;
+                continue;
+            }
+            // rejected: a new attempt of the same step
+            c.prev_reject = true;
+            h = forward ? hnew : -hnew;
+            c.reject = false;
+            if (a.max_rejects > 0 && nrej++ > a.max_rejects) {
                 st = ST_STEP_LIMIT;
-                break;
+                finish = true;
+            } else {
+                k = 0;
+                hh = h / c_bs.nseq[0];
+                for (int q = 0; q < kNv; q++) {
+                    ym[q] = ysav[q];
+                    yn[q] = ysav[q] + hh * dydx[q];
+                }
+                xnew = x + hh;
+                nn = 0;
+                continue;
             }
-            double hprev = hnext;
-            double htry = hnext;
-            bool clip = false;
-            if (x + htry >= tf) {
-                htry = tf - x;
-                clip = true;
+        } else {  // P_FINAL: the step is accepted
+            for (int q = 0; q < kNv; q++) dydx[q] = yd[q];
+            x += h;
+            const double hdid = h;
+            c.first_step = false;
+            int kopt;
+            if (k == 1) {
+                kopt = 2;
+            } else if (k <= k_targ) {
+                kopt = k;
+                if (work[k - 1] < KFAC1 * work[k]) kopt = k - 1;
+                else if (work[k] < KFAC2 * work[k - 1]) kopt = min(k + 1, KMAXX - 1);
+            } else {
+                kopt = k - 1;
+                if (k > 2 && work[k - 2] < KFAC1 * work[k - 1]) kopt = k - 2;
+                if (work[k] < KFAC2 * work[kopt]) kopt = min(k, KMAXX - 1);
             }
-            if (!(fabs(htry) > fabs(x) * 2.22045e-16)) {
-                st = ST_UNDERFLOW;
-                break;
+            if (c.prev_reject) {
+                k_targ = min(kopt, k);
+                hnew = fmin(fabs(h), hopt[k_targ]);
+                c.prev_reject = false;
+            } else {
+                if (kopt <= k) {
+                    hnew = hopt[kopt];
+                } else {
+                    if (k < k_targ && work[k] < KFAC2 * work[k - 1])
+                        hnew = hopt[k] * c_bs.cost[kopt + 1] / c_bs.cost[k];
+                    else
+                        hnew = hopt[k] * c_bs.cost[kopt] / c_bs.cost[k];
+                }
+                k_targ = kopt;
             }
-            double hn;
-            st = bs_step(f, a.uform, a.max_rejects, true, x, y, dydx, htry, hprev, c, hdid, hn, a.status);
-            if (st) break;
+            const double hn = forward ? hnew : -hnew;
             nacc++;
             hnext = clip ? fmax(hn, hprev) : hn;
             bool bad = false;
-            for (int k = 0; k < kNv; k++) bad |= !(y[k] == y[k]);
+            for (int q = 0; q < kNv; q++) bad |= !(y[q] == y[q]);
             if (bad) {
                 st = ST_NONFINITE;
-                break;
-            }
-            if (clip && fabs(hdid - htry) <= 4.0 * 2.22e-16 * fabs(tf)) {
-                x = tf;  // landed on the frame time
-                double g = gamma_of(a.uform, y);
-                atomicAdd(&a.espect[frame * a.nbins + ebin(a.ebin_thr, a.nbins, g - 1.0)], 1u);
-                // diffusion coefficients at the frame, src/diagnostics.c:659-705
-                double tt = x * 2.0 - t0 * 2.0 + a.t_end / a.nt_out;
-                double d0 = y0[0] - y[0], d1 = y0[1] - y[1], d2 = y0[2] - y[2];
-                double g0 = gamma_of(a.uform, y0);
-                double u[3], u0[3];
-                for (int k = 0; k < 3; k++) {
-                    u[k] = a.uform ? y[3 + k] : g * y[3 + k];
-                    u0[k] = a.uform ? y0[3 + k] : g0 * y0[3 + k];
+                finish = true;
+            } else {
+                if (clip && fabs(hdid - htry) <= 4.0 * 2.22e-16 * fabs(tf)) {
+                    x = tf;  // landed on the frame time
+                    frame_diagnostics(f, a, frame, x, t0, y, y0);
+                    frame++;
+                    if (frame < a.nt_out) tf = a.t_end * (frame + 1) / a.nt_out;
                 }
-                double du0 = u0[0] - u[0], du1 = u0[1] - u[1], du2 = u0[2] - u[2];
-                double e[6], e0[6];
-                emf64<TP_SYS_WLCS>(f, y[0], y[1], y[2], x, e, a.status);
-                emf64<TP_SYS_WLCS>(f, y0[0], y0[1], y0[2], t0, e0, a.status);
-                double mu = (e[0] * u[0] + e[1] * u[1] + e[2] * u[2]) /
-                            (sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
-                double mu0 = (e0[0] * u0[0] + e0[1] * u0[1] + e0[2] * u0[2]) /
-                             (sqrt(e0[0] * e0[0] + e0[1] * e0[1] + e0[2] * e0[2]) * sqrt(u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]));
-                double th = acos(mu) * 180 / TP_PI, th0 = acos(mu0) * 180 / TP_PI;
-                double v[8];
-                v[1] = d0 * d0 / tt; v[2] = d1 * d1 / tt; v[3] = d2 * d2 / tt;
-                v[0] = v[1] + v[2] + v[3];
-                v[4] = (du0 * du0 + du1 * du1 + du2 * du2) / tt;
-                v[5] = (mu - mu0) * (mu - mu0) / tt;
-                v[6] = (th - th0) * (th - th0) / tt;
-                v[7] = (g - g0) * (g - g0) / tt;
-                double* slot = a.dframe + (size_t)(frame + 1) * 8;
-                for (int k = 0; k < 8; k++) atomicAdd(slot + k, v[k]);
-                frame++;
-                if (frame < a.nt_out) tf = a.t_end * (frame + 1) / a.nt_out;
+                begin_step = true;
             }
         }
-        for (int k = 0; k < kNv; k++) a.y[kNv * i + k] = y[k];
-        a.t[i] = x;
-        a.h[i] = hnext;
-        a.steps[i] = nacc;
-        a.pstatus[i] = st;
-        if (st) atomicOr(a.status, st);
+        if (begin_step) {  // the checks before a step and the start of bs_step
+            if (frame >= a.nt_out) {
+                finish = true;
+            } else if (nacc >= a.max_steps) {
+                st = ST_STEP_LIMIT;
+                finish = true;
+            } else {
+                hprev = hnext;
+                htry = hnext;
+                clip = false;
+                if (x + htry >= tf) {
+                    htry = tf - x;
+                    clip = true;
+                }
+                if (!(fabs(htry) > fabs(x) * 2.22045e-16)) {
+                    st = ST_UNDERFLOW;
+                    finish = true;
+                } else {
+                    h = htry;
+                    k_targ = c_bs.k_targ0;
+                    k = 0;
+                    nrej = 0;
+                    forward = h > 0;
+                    work[0] = 0.0;
+                    for (int q = 0; q < kNv; q++) ysav[q] = y[q];
+                    if (h != hprev && !c.first_step) c.last_step = true;
+                    if (c.reject) {
+                        c.prev_reject = true;
+                        c.last_step = false;
+                    }
+                    c.reject = false;
+                    hnew = fabs(h);
+                    // first attempt
+                    h = forward ? hnew : -hnew;
+                    if (a.max_rejects > 0 && nrej++ > a.max_rejects) {
+                        st = ST_STEP_LIMIT;
+                        finish = true;
+                    } else {
+                        hh = h / c_bs.nseq[0];
+                        for (int q = 0; q < kNv; q++) {
+                            ym[q] = ysav[q];
+                            yn[q] = ysav[q] + hh * dydx[q];
+                        }
+                        xnew = x + hh;
+                        nn = 0;
+                        phase = P_MID;
+                    }
+                }
+            }
+        }
+        if (finish) {
+            for (int q = 0; q < kNv; q++) a.y[kNv * i + q] = y[q];
+            a.t[i] = x;
+            a.h[i] = hnext;
+            a.steps[i] = nacc;
+            a.pstatus[i] = st;
+            if (st) atomicOr(a.status, st);
+            i = atomicAdd(a.next, 1);
+            if (i < a.n) {
+                for (int q = 0; q < kNv; q++) {
+                    y[q] = a.y[kNv * i + q];
+                    y0[q] = a.y0[kNv * i + q];
+                }
+                x = a.t[i];
+                hnext = a.h[i];
+                phase = P_INIT;
+            }
+        }
     }
 }
 
@@ -409,6 +656,10 @@ static bool set_const(double atol, double rtol, int kmaxx)
             double ratio = (double)(h.nseq[k]) / h.nseq[l];
             h.coeff[k][l] = 1.0 / (ratio * ratio - 1.0);
         }
+    for (int k = 0; k < IMAXX; k++) {
+        h.expo[k] = 1.0 / (2 * k + 1);
+        h.facmin[k] = pow(0.02, h.expo[k]);  // STEPFAC3 of the step control
+    }
     h.kmaxx = kmaxx;
     h.atol = atol;
     h.rtol = rtol;
