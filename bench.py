@@ -21,6 +21,7 @@ import argparse
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -57,8 +58,8 @@ class Clocks:
         self.path = None
 
     def __enter__(self):
-        os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % self.device)
+        fd, self.path = tempfile.mkstemp(prefix="tp_clocks_%d_" % self.device, suffix=".csv")
+        os.close(fd)
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
