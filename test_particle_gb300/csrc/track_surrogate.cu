@@ -3,15 +3,19 @@
 // particles of a block at once as a chain of BF16 GEMMs on the 5th-generation
 // tensor cores (tcgen05.mma, FP32 accumulators in tensor memory).
 //
-// Block layout: 256 threads = two 128-row tiles; thread t owns row t % 128 of
-// tile t / 128 (its particle), which is also the tensor-memory lane its warp
-// may read.  Activations live in shared memory as the MMA A operand (128-byte
-// swizzled, K-major), one 64 KB buffer per tile, rewritten in place by each
-// layer's epilogue.  Weights are pre-packed in the same layout as 32 chunks
-// per evaluation (16 KB: 128 output rows x 64 inputs; the output layer 2 KB)
-// and stream from L2 through a 4-stage ring of shared buffers by 1-D bulk
-// async copies; thread 0 issues the copies and the MMAs, tracking the ring
-// with mbarriers, and every wait on them is bounded.
+// Block layout: 256 consumer threads = two 128-row tiles, one MMA warp and
+// three loader warps (three warps per SM sub-partition).  Consumer thread t
+// owns row t % 128 of tile t / 128 (its particle), which is also the
+// tensor-memory lane its warp may read.  Activations live in shared memory as
+// the MMA A operand (128-byte swizzled, K-major), one 64 KB buffer per tile,
+// rewritten in place by each layer's epilogue.  Weights are pre-packed in the
+// same layout as 32 chunks per evaluation (16 KB: 128 output rows x 64
+// inputs; the output layer 2 KB) and stream from L2 through a 4-stage ring
+// of shared buffers, copied by the loader warps with 16-byte cp.async (a
+// 1-D bulk copy engine moves at most about 25 B per cycle per SM; cp.async
+// from several warps several times that).  One thread of the MMA warp issues
+// the MMAs of both tiles per chunk; ring, accumulators and A operands are
+// handed over through mbarriers, and every wait on them is bounded.
 #include <cstring>
 
 #include "../../include/tp_gpu.h"
@@ -24,7 +28,11 @@ namespace tp {
 namespace mlp {
 
 constexpr int kTiles = 2;
-constexpr int kB = 128 * kTiles;         // particles (threads) per block
+constexpr int kB = 128 * kTiles;         // particles (consumer threads) per block
+constexpr int kLoaderWarps = 3;
+constexpr int kLoaders = 32 * kLoaderWarps;
+constexpr int kThreads = kB + 32 + kLoaders;  // + the MMA warp and the loader warps
+constexpr int kMmaWarp = kB / 32, kLoaderWarp0 = kB / 32 + 1;
 constexpr int kStages = 4;
 constexpr uint32_t kStageBytes = 16384;
 constexpr uint32_t kABytes = 128 * kHid * 2;  // one tile's activations (65536)
@@ -78,95 +86,152 @@ __device__ __forceinline__ uint32_t silu_half_bf16x2(float h0, float h1)
     return r;
 }
 
+// First chunk of each layer in the per-evaluation sequence (and the end).
+__host__ __device__ constexpr int layer_first_chunk(int l) { return l == 0 ? 0 : l < 5 ? 4 + 8 * (l - 1) : 32; }
+
 // Shared state of the block's tensor-core pipeline.
 struct Pipe {
     unsigned char* a[kTiles];        // activation tiles (A operands)
     uint32_t stage0;                 // shared address of stage 0
-    uint32_t full, empty, done;      // mbarrier addresses (full/empty: kStages each, 8 B apart)
+    uint32_t full, empty;            // ring mbarriers (kStages each, 8 B apart)
+    uint32_t accf, aready;           // a layer's accumulators complete / A operands written
+    uint32_t done;                   // MMA thread: every MMA it issued has completed
     uint32_t tmem;
-    int* abort;
+    int* abort;                      // a bounded wait ran out (or the MMA thread failed)
+    int* stop;                       // consumers are finished
     const float* bias;               // shared copy: 4 x 256 hidden biases then 6 output biases
     const float* hbias;              // halves of the 4 x 256 hidden biases
     const int* freq;
-    // thread 0 only: chunk counters (monotonic) and layer-completion count
-    uint32_t next_load, next_use, ndone;
 };
 
-// First chunk of each layer in the per-evaluation sequence (and the end).
-__host__ __device__ constexpr int layer_first_chunk(int l) { return l == 0 ? 0 : l < 5 ? 4 + 8 * (l - 1) : 32; }
-
-// Thread 0: the bulk copy of chunk c into its ring stage, once the MMAs that
-// read the stage's previous chunk have completed; false on a timed-out wait.
-__device__ __forceinline__ bool issue_load(uint32_t c, uint32_t full, uint32_t empty, uint32_t stage0,
-                                           const unsigned char* wpack)
+// Bounded wait that also gives up once the block has aborted; a wait that
+// runs out marks the block aborted.
+__device__ __forceinline__ bool wait_or_abort(uint32_t bar, uint32_t parity, int* abort)
 {
-    const uint32_t s = c % kStages, use = c / kStages;
-    if (use > 0 && !tc::mbar_wait(empty + 8 * s, (use - 1) & 1, kWaitLimit)) return false;
-    const Chunk ch = chunk_of((int)(c % kChunks));
-    tc::mbar_expect_tx(full + 8 * s, ch.bytes);
-    tc::bulk_g2s(stage0 + s * kStageBytes, wpack + ch.offset, ch.bytes, full + 8 * s);
-    return true;
+    for (uint32_t it = 0; it < kWaitLimit; it++) {
+        if (tc::mbar_try_wait(bar, parity)) return true;
+        if ((it & 63u) == 63u && *(volatile int*)abort) return false;
+    }
+    *(volatile int*)abort = 1;
+    return false;
 }
 
-// Thread 0: the MMAs of one layer.  Hidden layers go by k-atom: its two
-// output halves sit in adjacent stages (a stage pair), and each MMA covers
-// N = 256 outputs; after issuing a pair it refills the other pair, whose MMAs
-// were issued one step earlier.  The output layer (N = 16) goes chunk by
-// chunk.  Ring state in registers; descriptors built once and advanced by
-// adding to their start-address field (16-byte units).
-__device__ __noinline__ void issue_layer(Pipe& pp, const unsigned char* wpack, int layer)
+// The loader warps: stream the weight chunks in use order into the ring
+// with 16-byte cp.async (per SM several times the rate of 1-D bulk copies).
+// Loader warp w takes every kLoaderWarps-th chunk starting at w, waits until
+// the MMAs that read the stage's previous chunk have completed, copies the
+// chunk (each lane every 32nd piece), waits for its copies, fences them for
+// the tensor core and signals the stage (32 arrivals on `full`).  So up to
+// kLoaderWarps chunks are in flight and each is signalled as soon as it has
+// landed.  Ends on `stop` or an abort.
+__device__ __noinline__ void loader(const Pipe& pp, const unsigned char* wpack)
 {
-    const bool last = layer == kLayers - 1;
-    const uint32_t idesc = tc::idesc_bf16_f32(128, last ? 16 : 256);
-    const uint32_t full = pp.full, empty = pp.empty, stage0 = pp.stage0, tmem = pp.tmem;
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x / 32 - kLoaderWarp0;
+    for (uint32_t u = w;; u += kLoaderWarps) {
+        const uint32_t s = u % kStages, use = u / kStages;
+        if (use > 0) {
+            bool ok = false;
+            for (uint32_t it = 0; it < kWaitLimit && !ok; it++) {
+                ok = tc::mbar_try_wait(pp.empty + 8 * s, (use - 1) & 1);
+                if (!ok && (it & 63u) == 63u && (*(volatile int*)pp.abort || *(volatile int*)pp.stop)) break;
+            }
+            if (!ok) {
+                if (!*(volatile int*)pp.stop) *(volatile int*)pp.abort = 1;
+                break;
+            }
+        }
+        const Chunk ch = chunk_of((int)(u % kChunks));
+        const unsigned char* src = wpack + ch.offset;
+        const uint32_t dst = pp.stage0 + s * kStageBytes;
+        for (uint32_t off = lane * 16; off < ch.bytes; off += 512)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + off), "l"(src + off) : "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        tc::fence_async_smem();
+        tc::mbar_arrive(pp.full + 8 * s);
+    }
+}
+
+// The MMA thread (lane 0 of the MMA warp).  Per layer: wait until the
+// consumers of both tiles have written their A operands (and read the
+// previous accumulators), then read the layer's weights from the ring: hidden
+// layers by k-atom, both output halves (adjacent stages) in one N = 256 MMA
+// per tile; the output layer (N = 16) chunk by chunk; commit to `accf`.  Ends
+// when the consumers raise `stop` (or on a failed wait), after the MMAs it
+// issued have completed (bounded wait).
+__device__ __noinline__ void mma_issuer(const Pipe& pp, int* status)
+{
+    uint32_t next_use = 0, nready = 0;
+    bool ok = true, stopped = false;
     uint64_t adesc[kTiles];
 #pragma unroll
     for (int t = 0; t < kTiles; t++) adesc[t] = tc::desc_sw128(tc::smem_addr(pp.a[t]));
-    uint32_t next_use = pp.next_use, next_load = pp.next_load;
-    const uint32_t base = next_use - (next_use % kChunks);
-    const uint32_t c_end = base + (uint32_t)layer_first_chunk(layer + 1);
-    const uint32_t width = last ? 1u : 2u;  // chunks per MMA group
-    bool ok = !*pp.abort;
-    for (uint32_t c = next_use; ok && c < c_end; c += width) {
-        const uint32_t s = c % kStages;
-        for (uint32_t w = 0; w < width && ok; w++)
-            ok = tc::mbar_wait(full + 8 * ((c + w) % kStages), ((c + w) / kStages) & 1, kWaitLimit);
-        if (!ok) break;
-        tc::tc_fence_after();
-        const Chunk ch = chunk_of((int)(c % kChunks));
-        const uint64_t bdesc = tc::desc_sw128(stage0 + s * kStageBytes);
+    while (ok) {
+        for (int l = 0; ok && l < kLayers; l++) {
+            ok = wait_or_abort(pp.aready, nready & 1, pp.abort);
+            nready++;
+            if (ok && *(volatile int*)pp.stop) {
+                stopped = true;
+                ok = false;
+            }
+            if (!ok) break;
+            tc::tc_fence_after();
+            const bool last = l == kLayers - 1;
+            const uint32_t idesc = tc::idesc_bf16_f32(128, last ? 16 : 256);
+            const uint32_t width = last ? 1u : 2u;
+            const uint32_t c_end = next_use + (uint32_t)(layer_first_chunk(l + 1) - layer_first_chunk(l));
+            for (uint32_t c = next_use; ok && c < c_end; c += width) {
+                for (uint32_t w = 0; w < width && ok; w++)
+                    ok = wait_or_abort(pp.full + 8 * ((c + w) % kStages), ((c + w) / kStages) & 1, pp.abort);
+                if (!ok) break;
+                tc::tc_fence_after();
+                const Chunk ch = chunk_of((int)(c % kChunks));
+                const uint64_t bdesc = tc::desc_sw128(pp.stage0 + (c % kStages) * kStageBytes);
 #pragma unroll
-        for (int t = 0; t < kTiles; t++) {
-            const uint64_t a = adesc[t] + (uint64_t)(ch.katom * (128 * 128 / 16));
-            const uint32_t d = tmem + (uint32_t)(t * 256);
+                for (int t = 0; t < kTiles; t++) {
+                    const uint64_t a = adesc[t] + (uint64_t)(ch.katom * (128 * 128 / 16));
+                    const uint32_t d = pp.tmem + (uint32_t)(t * 256);
 #pragma unroll
-            for (int kk = 0; kk < 4; kk++)
-                tc::mma_bf16(d, a + 2 * kk, bdesc + 2 * kk, idesc, (ch.katom | kk) != 0);
-        }
-        for (uint32_t w = 0; w < width; w++) tc::mma_commit(empty + 8 * ((c + w) % kStages));
-        next_use = c + width;
-        // refill up to one stage pair ahead of the next group
-        while (ok && next_load < next_use + kStages - width) {
-            ok = issue_load(next_load, full, empty, stage0, wpack);
-            if (ok) next_load++;
+                    for (int kk = 0; kk < 4; kk++)
+                        tc::mma_bf16(d, a + 2 * kk, bdesc + 2 * kk, idesc, (ch.katom | kk) != 0);
+                }
+                for (uint32_t w = 0; w < width; w++) tc::mma_commit(pp.empty + 8 * ((c + w) % kStages));
+                next_use = c + width;
+            }
+            tc::mma_commit(pp.accf);
         }
     }
-    pp.next_use = next_use;
-    pp.next_load = next_load;
-    if (!ok) *pp.abort = 1;
+    // drain: the MMAs issued so far
     tc::mma_commit(pp.done);
+    const bool fine = tc::mbar_wait(pp.done, 0, kWaitLimit);
+    if (!stopped || !fine) {
+        *(volatile int*)pp.abort = 1;
+        atomicOr(status, ST_TIMEOUT);
+    }
 }
 
-// All kB threads call this together; each passes its own position and
-// receives the model's E and B there.  Returns zeros once the pipeline aborted.
-__device__ __noinline__ void field_block(const Model& md, Pipe& pp, const uint64_t X[3], float E[3],
-                                         float B[3])
+// Barrier of the kB consumer threads (the MMA and loader warps never join it).
+__device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kB) : "memory"); }
+
+// Per-thread position in the accumulator barrier's phases.
+struct Cons {
+    uint32_t nacc = 0;
+};
+
+// Consumer side of one field evaluation: every consumer thread of the block
+// calls this together with its own position and receives the model's E and
+// B there.  Per layer it waits for the accumulators, turns its row into the
+// next layer's A operand and signals `aready`.  After an abort every wait
+// returns at once and the values are meaningless (the caller discards them).
+__device__ __noinline__ void field_tile(const Model& md, const Pipe& pp, Cons& cs, const uint64_t X[3],
+                                        float E[3], float B[3])
 {
     const int tid = threadIdx.x, warp = tid >> 5;
     const int tile = tid >> 7, row = tid & 127;
     unsigned char* arow = pp.a[tile];
     const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
     const uint32_t tcol = pp.tmem + lane_base + (uint32_t)(tile * 256);
+    const uint32_t accf = pp.accf, aready = pp.aready;
     // Fourier features of this thread's particle: inputs 0..63 sin, 64..127 cos
     {
         const uint32_t U0 = (uint32_t)(X[0] >> 32), U1 = (uint32_t)(X[1] >> 32), U2 = (uint32_t)(X[2] >> 32);
@@ -193,21 +258,11 @@ __device__ __noinline__ void field_block(const Model& md, Pipe& pp, const uint64
     }
     tc::fence_async_smem();
     tc::tc_fence_before();
-    __syncthreads();
+    tc::mbar_arrive(aready);
     for (int l = 0; l < kLayers; l++) {
-        if (tid == 0) {
-            tc::tc_fence_after();
-            if (!*pp.abort) issue_layer(pp, md.wpack, l);
-            if (!*pp.abort && !tc::mbar_wait(pp.done, pp.ndone & 1, kWaitLimit)) *pp.abort = 1;
-            pp.ndone++;
-        }
-        __syncthreads();
+        wait_or_abort(accf, cs.nacc & 1, pp.abort);
+        cs.nacc++;
         tc::tc_fence_after();
-        if (*pp.abort) {
-            E[0] = E[1] = E[2] = 0.f;
-            B[0] = B[1] = B[2] = 0.f;
-            return;
-        }
         if (l < kLayers - 1) {
             // SiLU(z) = h + h tanh(h), h = z / 2 = acc / 2 + bias / 2, in packed
             // BF16 pairs (one tanh per two values); the result is already the
@@ -233,6 +288,8 @@ __device__ __noinline__ void field_block(const Model& md, Pipe& pp, const uint64
                     make_uint4(pk[4], pk[5], pk[6], pk[7]);
             }
             tc::fence_async_smem();
+            tc::tc_fence_before();
+            tc::mbar_arrive(aready);
         } else {
             float v[16];
             tc::tmem_ld16(tcol, v);
@@ -243,21 +300,21 @@ __device__ __noinline__ void field_block(const Model& md, Pipe& pp, const uint64
             E[0] = (v[3] + bo[3]) * md.out_scale[3] + md.out_shift[3];
             E[1] = (v[4] + bo[4]) * md.out_scale[4] + md.out_shift[4];
             E[2] = (v[5] + bo[5]) * md.out_scale[5] + md.out_shift[5];
+            tc::tc_fence_before();
         }
-        tc::tc_fence_before();
-        __syncthreads();
     }
 }
 
 // Block set-up shared by the kernels: shared layout, biases and frequencies,
-// mbarriers, tensor memory, and the first chunks in flight.
+// mbarriers and tensor memory.
 struct SmemStatic {
     float bias[kLayers * kHid];
     __align__(16) float hbias[(kLayers - 1) * kHid];
     int freq[3 * kFeat];
-    uint64_t bars[2 * kStages + 1];
+    uint64_t bars[2 * kStages + 3];
     uint32_t tmem_slot;
     int abort;
+    int stop;
 };
 
 __device__ void pipe_setup(Pipe& pp, SmemStatic& st, unsigned char* dyn, const Model& md)
@@ -275,18 +332,23 @@ __device__ void pipe_setup(Pipe& pp, SmemStatic& st, unsigned char* dyn, const M
     for (int k = tid; k < 3 * kFeat; k += blockDim.x) st.freq[k] = md.freq[k];
     pp.full = tc::smem_addr(&st.bars[0]);
     pp.empty = tc::smem_addr(&st.bars[kStages]);
-    pp.done = tc::smem_addr(&st.bars[2 * kStages]);
+    pp.accf = tc::smem_addr(&st.bars[2 * kStages]);
+    pp.aready = tc::smem_addr(&st.bars[2 * kStages + 1]);
+    pp.done = tc::smem_addr(&st.bars[2 * kStages + 2]);
     pp.abort = &st.abort;
+    pp.stop = &st.stop;
     pp.bias = st.bias;
     pp.hbias = st.hbias;
     pp.freq = st.freq;
-    pp.next_load = pp.next_use = pp.ndone = 0;
     if (tid == 0) {
         st.abort = 0;
+        st.stop = 0;
         for (int s = 0; s < kStages; s++) {
-            tc::mbar_init(pp.full + 8 * s, 1);
+            tc::mbar_init(pp.full + 8 * s, 32);
             tc::mbar_init(pp.empty + 8 * s, 1);
         }
+        tc::mbar_init(pp.accf, 1);
+        tc::mbar_init(pp.aready, kB);
         tc::mbar_init(pp.done, 1);
         tc::mbar_fence_init();
     }
@@ -298,35 +360,54 @@ __device__ void pipe_setup(Pipe& pp, SmemStatic& st, unsigned char* dyn, const M
     __syncthreads();
     tc::tc_fence_after();
     pp.tmem = st.tmem_slot;
-    if (tid == 0)
-        for (; pp.next_load < (uint32_t)(kStages - 1); pp.next_load++)
-            issue_load(pp.next_load, pp.full, pp.empty, pp.stage0, md.wpack);
 }
 
-// Waits (bounded) for the copies still in flight, then frees tensor memory.
-__device__ void pipe_teardown(Pipe& pp, int* status)
+// Consumers, after their last evaluation: raise `stop` and release the
+// MMA thread from its wait for the next A operands.
+__device__ void consumers_finish(const Pipe& pp)
 {
-    const int tid = threadIdx.x;
-    if (tid == 0) {
-        bool ok = !*pp.abort;
-        for (uint32_t c = pp.next_use; c < pp.next_load; c++) {
-            const uint32_t s = c % kStages, use = c / kStages;
-            if (!tc::mbar_wait(pp.full + 8 * s, use & 1, kWaitLimit)) ok = false;
-        }
-        if (!ok) atomicOr(status, ST_TIMEOUT);
-    }
+    consumers_sync();
+    if (threadIdx.x == 0) *(volatile int*)pp.stop = 1;
+    consumers_sync();
+    tc::mbar_arrive(pp.aready);
+}
+
+// Every thread, at the end: frees tensor memory once the MMA thread has
+// drained its MMAs and the loaders their copies.
+__device__ void pipe_teardown(const Pipe& pp)
+{
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
-    if ((tid >> 5) == 0) tc::tmem_dealloc(pp.tmem, kTmemCols);
+    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(pp.tmem, kTmemCols);
+}
+
+__device__ __forceinline__ void consumers_diff_sum(const double sg[8], double* red, double* slot)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        double v = sg[c];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) red[warp * 8 + c] = v;
+    }
+    consumers_sync();
+    if (threadIdx.x < 8) {
+        double s = 0.0;
+        for (int w = 0; w < kB / 32; w++) s += red[w * 8 + threadIdx.x];
+        slot[threadIdx.x] += s;
+    }
+    consumers_sync();
 }
 
 // Fixed-step tracking with the learned field (src/tracking.c:297-462
-// schedule and diagnostics); every thread runs every step so that the
-// block-wide field evaluations line up; inactive and escaped particles
-// evaluate at their frozen position and discard the result.
-__global__ void __launch_bounds__(kB, 1) track_surrogate_kernel(mixed::MixField f, Model md,
-                                                                 TrackBufs b, TrackParams q)
+// schedule and diagnostics); every consumer thread runs every step so that
+// the field evaluations line up; inactive and escaped particles evaluate at
+// their frozen position and discard the result.  Threads 0..kB-1 own one
+// particle each; then the MMA warp and the loader warps.
+__global__ void __launch_bounds__(kThreads, 1) track_surrogate_kernel(mixed::MixField f, Model md,
+                                                                       TrackBufs b, TrackParams q)
 {
     using namespace mixed;
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
@@ -335,11 +416,19 @@ __global__ void __launch_bounds__(kB, 1) track_surrogate_kernel(mixed::MixField 
     __shared__ unsigned int hist[kSurrSmemBins];
     Pipe pp;
     pipe_setup(pp, st, smem_dyn, md);
+    if (threadIdx.x >= kB) {
+        if (threadIdx.x / 32 >= kLoaderWarp0) loader(pp, md.wpack);
+        else if (threadIdx.x == kMmaWarp * 32) mma_issuer(pp, b.status);
+        __syncwarp();
+        pipe_teardown(pp);
+        return;
+    }
     const bool smem_hist = q.nbins <= kSurrSmemBins;
     const float dt = (float)q.dt;
     const int ntiles = (q.n + kB - 1) / kB;
-    auto field = [&](const uint64_t* X, float* E, float* B) { field_block(md, pp, X, E, B); };
-    for (int tile = blockIdx.x; tile < ntiles && !st.abort; tile += gridDim.x) {
+    Cons cs;
+    auto field = [&](const uint64_t* X, float* E, float* B) { field_tile(md, pp, cs, X, E, B); };
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int i = tile * kB + threadIdx.x;
         const bool active = i < q.n;
         PM p = {};
@@ -385,7 +474,7 @@ __global__ void __launch_bounds__(kB, 1) track_surrogate_kernel(mixed::MixField 
         int to_diff = kDiffInterval - q.sstep % kDiffInterval;
         if (to_frame == q.einterval) to_frame = 0;
         if (to_diff == kDiffInterval) to_diff = 0;
-        for (int j = q.sstep; j <= q.estep && !st.abort; j++) {
+        for (int j = q.sstep; j <= q.estep; j++) {
             const bool at_diff = to_diff == 0, at_frame = to_frame == 0;
             to_diff = at_diff ? kDiffInterval - 1 : to_diff - 1;
             to_frame = at_frame ? q.einterval - 1 : to_frame - 1;
@@ -393,14 +482,14 @@ __global__ void __launch_bounds__(kB, 1) track_surrogate_kernel(mixed::MixField 
             const bool push = active && (esc_pre == 0 || f.bc_flag == 0);
             PM pn = p;
             bool e2 = false;
-            wirz_f32(f, pn, dt, field, e2);  // block-wide: every thread evaluates
+            wirz_f32(f, pn, dt, field, e2);  // every consumer thread evaluates
             if (push) {
                 p = pn;
                 if (e2) esc_after = 1;
                 nst += 1;
                 done += 1;
             }
-            if (at_diff) {  // block-uniform: one more block-wide field evaluation
+            if (at_diff) {  // block-uniform: one more field evaluation
                 float E[3], B[3];
                 field(p.X, E, B);
                 if (push && esc_after == 0) {
@@ -435,12 +524,12 @@ __global__ void __launch_bounds__(kB, 1) track_surrogate_kernel(mixed::MixField 
                 if (ntp < q.nt_out) {
                     bool take = active && esc_after == 0;
                     if (smem_hist) {
-                        __syncthreads();
-                        for (int k = threadIdx.x; k < q.nbins; k += blockDim.x) hist[k] = 0u;
-                        __syncthreads();
+                        consumers_sync();
+                        for (int k = threadIdx.x; k < q.nbins; k += kB) hist[k] = 0u;
+                        consumers_sync();
                         if (take) atomicAdd(&hist[energy_bin_f(b.ebin_thr, q.nbins, p.u)], 1u);
-                        __syncthreads();
-                        for (int k = threadIdx.x; k < q.nbins; k += blockDim.x)
+                        consumers_sync();
+                        for (int k = threadIdx.x; k < q.nbins; k += kB)
                             if (hist[k]) atomicAdd(&b.espect[ntp * q.nbins + k], hist[k]);
                     } else if (take) {
                         atomicAdd(&b.espect[ntp * q.nbins + energy_bin_f(b.ebin_thr, q.nbins, p.u)], 1u);
@@ -449,13 +538,13 @@ __global__ void __launch_bounds__(kB, 1) track_surrogate_kernel(mixed::MixField 
                 ntp++;
             }
             if (at_diff) {
-                block_diff_sum(sg, red, slot_base + (size_t)tstep * 8);
+                consumers_diff_sum(sg, red, slot_base + (size_t)tstep * 8);
                 tstep++;
             }
             if (active && esc_after && at_diff && tstep < q.nsdc) atomicSub(&b.remain[tstep], 1);
             esc_pre = esc_after;
         }
-        if (active && !st.abort) {
+        if (active && !*(volatile int*)&st.abort) {
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 double xk = f.min[k] + f.L[k] * ((double)p.X[k] * 5.421010862427522e-20);
@@ -468,32 +557,42 @@ __global__ void __launch_bounds__(kB, 1) track_surrogate_kernel(mixed::MixField 
             b.t[i] = tstart + done * q.dt;
             b.nsteps_ptl[i] = nst;
         }
-        __syncthreads();
+        consumers_sync();
     }
-    pipe_teardown(pp, b.status);
+    consumers_finish(pp);
+    pipe_teardown(pp);
 }
 
 // Model field at n positions through the in-kernel (per-block) evaluation path.
-__global__ void __launch_bounds__(kB, 1) field_eval_kernel(Model md, const uint32_t* __restrict__ U,
-                                                           int n, float* __restrict__ out, int* status)
+__global__ void __launch_bounds__(kThreads, 1) field_eval_kernel(Model md, const uint32_t* __restrict__ U,
+                                                                  int n, float* __restrict__ out, int* status)
 {
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
     __shared__ SmemStatic st;
     Pipe pp;
     pipe_setup(pp, st, smem_dyn, md);
-    for (int tile = blockIdx.x; tile * kB < n && !st.abort; tile += gridDim.x) {
+    if (threadIdx.x >= kB) {
+        if (threadIdx.x / 32 >= kLoaderWarp0) loader(pp, md.wpack);
+        else if (threadIdx.x == kMmaWarp * 32) mma_issuer(pp, status);
+        __syncwarp();
+        pipe_teardown(pp);
+        return;
+    }
+    Cons cs;
+    for (int tile = blockIdx.x; tile * kB < n; tile += gridDim.x) {
         int i = tile * kB + threadIdx.x;
         uint64_t X[3] = {0, 0, 0};
         if (i < n)
             for (int k = 0; k < 3; k++) X[k] = (uint64_t)U[3 * i + k] << 32;
         float E[3], B[3];
-        field_block(md, pp, X, E, B);
-        if (i < n && !st.abort) {
+        field_tile(md, pp, cs, X, E, B);
+        if (i < n && !*(volatile int*)&st.abort) {
             out[6 * i] = B[0]; out[6 * i + 1] = B[1]; out[6 * i + 2] = B[2];
             out[6 * i + 3] = E[0]; out[6 * i + 4] = E[1]; out[6 * i + 5] = E[2];
         }
     }
-    pipe_teardown(pp, status);
+    consumers_finish(pp);
+    pipe_teardown(pp);
 }
 
 // Packs the BF16 weights [out_pad][in] of every layer into the chunk layout above.
@@ -527,7 +626,7 @@ cudaError_t launch_track_surrogate(const mixed::MixField& f, const Model& md, co
     cudaError_t e = cudaFuncSetAttribute(track_surrogate_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDyn);
     if (e != cudaSuccess) return e;
-    track_surrogate_kernel<<<grid, kB, kSmemDyn, s>>>(f, md, b, q);
+    track_surrogate_kernel<<<grid, kThreads, kSmemDyn, s>>>(f, md, b, q);
     return cudaGetLastError();
 }
 
@@ -553,7 +652,7 @@ extern "C" int tp_mlp_eval_kernel(int n, const unsigned int* u, float* out6)
     if (ok) {
         int grid = (n + mlp::kB - 1) / mlp::kB;
         if (grid > g.num_sms) grid = g.num_sms;
-        mlp::field_eval_kernel<<<grid, mlp::kB, mlp::kSmemDyn, s>>>(md, dU, n, dO, g.d_status);
+        mlp::field_eval_kernel<<<grid, mlp::kThreads, mlp::kSmemDyn, s>>>(md, dU, n, dO, g.d_status);
         ok = cuda_ok(cudaGetLastError(), "field eval");
     }
     if (ok) {
