@@ -271,21 +271,22 @@ __device__ __noinline__ void field_tile(const Model& md, const Pipe& pp, Cons& c
             const uint32_t rbase = (uint32_t)(row >> 3) * 1024u + (uint32_t)(row & 7) * 128u;
             const uint32_t rx = (uint32_t)(row & 7);
 #pragma unroll 1
-            for (int c0 = 0; c0 < kHid; c0 += 16) {
-                float v[16];
-                tc::tmem_ld16(tcol + (uint32_t)c0, v);
-                uint32_t pk[8];
+            for (int c0 = 0; c0 < kHid; c0 += 32) {
+                float v[32];
+                tc::tmem_ld32(tcol + (uint32_t)c0, v);
+                uint32_t pk[16];
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
+                for (int q = 0; q < 8; q++) {
                     const float4 hb = hb4[(c0 >> 2) + q];
                     pk[2 * q] = silu_half_bf16x2(fmaf(0.5f, v[4 * q], hb.x), fmaf(0.5f, v[4 * q + 1], hb.y));
                     pk[2 * q + 1] = silu_half_bf16x2(fmaf(0.5f, v[4 * q + 2], hb.z), fmaf(0.5f, v[4 * q + 3], hb.w));
                 }
-                // 128-byte-swizzled row chunk positions of columns c0 and c0 + 8
+                // 128-byte-swizzled row chunk positions of columns c0, c0 + 8, c0 + 16, c0 + 24
                 const uint32_t atom = (uint32_t)(c0 >> 6) * 16384u, ch = (uint32_t)((c0 >> 3) & 7);
-                *reinterpret_cast<uint4*>(arow + atom + rbase + ((ch ^ rx) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                *reinterpret_cast<uint4*>(arow + atom + rbase + (((ch + 1) ^ rx) << 4)) =
-                    make_uint4(pk[4], pk[5], pk[6], pk[7]);
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    *reinterpret_cast<uint4*>(arow + atom + rbase + (((ch + k) ^ rx) << 4)) =
+                        make_uint4(pk[4 * k], pk[4 * k + 1], pk[4 * k + 2], pk[4 * k + 3]);
             }
             tc::fence_async_smem();
             tc::tc_fence_before();
