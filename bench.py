@@ -34,10 +34,10 @@ METRIC = "particle-pushes/s on 1 GB300: FP64 vs mixed+surrogate at stated spectr
 UNIT = "pushes/s"
 # DRAM bytes (read + write) per push of track_mixed_kernel<4>, from one ncu
 # capture of `python bench.py --profile mixed` (256^3 grid, 131072 particles,
-# 200 steps: 2.136 GB for 26,214,400 pushes); the headline workload has the
+# 200 steps: 2.130 GB for 26,214,400 pushes); the headline workload has the
 # same particle density per cell, so its traffic scales with the pushes.
 # Summary: profiles/track_mixed_kernel_pic_256cube_131072ptl.txt
-DRAM_BYTES_PER_PUSH = (2.124449e9 + 11.355648e6) / 26214400.0
+DRAM_BYTES_PER_PUSH = (2.119457e9 + 10.865920e6) / 26214400.0
 
 
 def peaks():
