@@ -52,15 +52,11 @@ __device__ __forceinline__ void cell_of(uint64_t X, int n, int& i, float& fr)
 
 // The eight corner nodes of the cell a particle last sampled, kept in
 // registers: at a few tenths of a cell per step most evaluations fall in the
-// same cell as the previous one and need no memory traffic at all.  Optionally
-// a shared-memory slot into which the corners of the cell the particle is
-// expected to enter next are being copied.
+// same cell as the previous one and need no memory traffic at all.
 template <int STRIDE>
 struct CellCache {
-    uint32_t key = 0xffffffffu;   // node index of the cached cell (grids hold < 2^32 - 1 nodes)
+    uint32_t key = 0xffffffffu;  // node index of the cached cell (grids hold < 2^32 - 1 nodes)
     float4 c[8 * STRIDE];
-    uint32_t skey = 0xffffffffu;  // cell whose corners are being copied into `slot`
-    float4* slot = nullptr;       // this thread's slot: 8 * STRIDE float4 at a stride of kBlock
 };
 
 // trilinear interpolation of a node-interleaved field with `stride` float4s per node
@@ -83,11 +79,6 @@ __device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __r
     const uint32_t base = ix + nx * iy + nxy * iz;
     if (base != cc.key) {
         const float4* p = g + (size_t)base * STRIDE;
-        if (cc.slot && base == cc.skey) {  // prefetched: wait for this thread's copies
-            asm volatile("cp.async.wait_all;" ::: "memory");
-#pragma unroll
-            for (int i = 0; i < 8 * STRIDE; i++) cc.c[i] = cc.slot[i * kBlock];
-        } else
 #pragma unroll
         for (int c = 0; c < STRIDE; c++) {
             cc.c[0 * STRIDE + c] = __ldg(p + c);
@@ -117,35 +108,6 @@ __device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __r
         }
         out[c] = r;
     }
-}
-
-// Starts copying (cp.async, 16 bytes per copy) the corners of the cell
-// containing X into the thread's shared slot, unless it is the cell in the
-// registers or the one already in the slot.  The indices come from a wrapped
-// fixed-point position, so every corner lies inside the grid.
-template <int STRIDE>
-__device__ __forceinline__ void slot_fill(const MixField& f, const float4* g, const uint64_t X[3],
-                                          CellCache<STRIDE>& cc)
-{
-    const uint32_t ix = (uint32_t)(((X[0] >> 32) * (uint64_t)(uint32_t)(f.nx - 1)) >> 32);
-    const uint32_t iy = (uint32_t)(((X[1] >> 32) * (uint64_t)(uint32_t)(f.ny - 1)) >> 32);
-    const uint32_t iz = (uint32_t)(((X[2] >> 32) * (uint64_t)(uint32_t)(f.nz - 1)) >> 32);
-    const uint32_t nx = f.nx, nxy = (uint32_t)f.nx * f.ny;
-    const uint32_t base = ix + nx * iy + nxy * iz;
-    if (!cc.slot || base == cc.key || base == cc.skey) return;
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    const float4* p = g + (size_t)base * STRIDE;
-    const uint32_t off[8] = {0, 1, nx, nx + 1, nxy, nxy + 1, nxy + nx, nxy + nx + 1};
-#pragma unroll
-    for (int k = 0; k < 8; k++)
-#pragma unroll
-        for (int c = 0; c < STRIDE; c++) {
-            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(cc.slot + (k * STRIDE + c) * kBlock);
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(p + (size_t)off[k] * STRIDE + c)
-                         : "memory");
-        }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    cc.skey = base;
 }
 
 // Per-particle register state of the field evaluation.
@@ -202,14 +164,6 @@ __device__ __forceinline__ void field_mixed(const MixField& f, const uint64_t X[
         B[0] = b0; B[1] = b1; B[2] = f.mB0 + b2;
         E[0] = e0; E[1] = e1; E[2] = e2;
     }
-}
-
-// Before the second field evaluation of a step: prefetch the cell the step is
-// expected to end in (gridded E, B only).
-template <int SYS>
-__device__ __forceinline__ void field_ahead(const MixField& f, const uint64_t Xe[3], FieldCache& fc)
-{
-    if (SYS == TP_SYS_PIC) slot_fill<2>(f, f.eb, Xe, fc.eb);
 }
 
 }  // namespace mixed

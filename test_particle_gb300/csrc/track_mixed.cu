@@ -47,11 +47,7 @@ template <int SYS>
 __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, TrackBufs b, TrackParams q)
 {
     __shared__ double red[(kBlock / 32) * 8];
-    // gridded fields: a prefetch slot per thread (32 KB per block), paid for
-    // by a smaller shared histogram (more bins go to global atomics)
-    constexpr int kMixBins = SYS == TP_SYS_PIC ? 512 : kMaxSmemBins;
-    __shared__ float4 slot_mem[SYS == TP_SYS_PIC ? 16 : 1][kBlock];
-    __shared__ unsigned int hist[kMixBins];
+    __shared__ unsigned int hist[kMaxSmemBins];
     __shared__ double dg[DG_ROWS][kBlock];
     extern __shared__ ModeF smodes[];
     if (SYS == TP_SYS_MODESUM) {
@@ -59,14 +55,13 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
         __syncthreads();
     }
     const int tx = threadIdx.x;
-    const bool smem_hist = q.nbins <= kMixBins;
+    const bool smem_hist = q.nbins <= kMaxSmemBins;
     const float dt = (float)q.dt;
     for (int tile = blockIdx.x; tile < q.ntiles; tile += gridDim.x) {
         const int i = tile * kBlock + tx;
         const bool active = i < q.n;
         PM p = {};
         FieldCache fc;
-        if (SYS == TP_SYS_PIC) fc.eb.slot = &slot_mem[0][tx];
         int nst = 1;
         bool esc = false;
 #pragma unroll
@@ -116,9 +111,9 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
             to_frame = at_frame ? q.einterval - 1 : to_frame - 1;
             if (active && (esc_pre == 0 || f.bc_flag == 0)) {
                 bool e2 = false;
-                wirz_f32(
-                    f, p, dt, [&](const uint64_t* X, float* E, float* B) { field_mixed<SYS>(f, X, E, B, smodes, fc); },
-                    e2, [&](const uint64_t* Xe) { field_ahead<SYS>(f, Xe, fc); });
+                wirz_f32(f, p, dt, [&](const uint64_t* X, float* E, float* B) {
+                    field_mixed<SYS>(f, X, E, B, smodes, fc);
+                }, e2);
                 if (e2) esc_after = 1;
                 nst += 1;
                 done += 1;
@@ -196,7 +191,6 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
             b.nsteps_ptl[i] = nst;
         }
     }
-    asm volatile("cp.async.wait_all;" ::: "memory");  // no copy may outlive the block's shared memory
 }
 
 // --------------------------------------------------------------- launchers

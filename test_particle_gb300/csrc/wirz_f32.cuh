@@ -41,16 +41,10 @@ __device__ __forceinline__ void advance(uint64_t& X, int& img, float fr)
     X = nx;
 }
 
-struct NoAhead {
-    __device__ __forceinline__ void operator()(const uint64_t*) const {}
-};
-
-// One Wirz push; field(X, E, B) evaluates the field at a fixed-point position;
-// ahead(P) is told the expected end of the step (straight-line extrapolation
-// of the half-step displacement) before the second evaluation.
-template <class FieldFn, class AheadFn = NoAhead>
+// One Wirz push; field(X, E, B) evaluates the field at a fixed-point position.
+template <class FieldFn>
 __device__ __forceinline__ void wirz_f32(const MixField& f, PM& p, float dt, FieldFn&& field,
-                                         bool& escaped, AheadFn&& ahead = AheadFn())
+                                         bool& escaped)
 {
     // Norms and their inverses come from one rsqrt each (a single SFU
     // operation, a few ulp): the FP32 path's error budget is set by FP32
@@ -82,14 +76,9 @@ __device__ __forceinline__ void wirz_f32(const MixField& f, PM& p, float dt, Fie
     float dpre[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) dpre[k] = (h[k] * a1 + hp[k] * a2 + hr[k] * a3) * f.invL[k];
-    uint64_t Xp[3], Xe[3];
+    uint64_t Xp[3] = {p.X[0], p.X[1], p.X[2]};
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const uint64_t d = (uint64_t)float_to_fx(dpre[k]);
-        Xp[k] = p.X[k] + d;
-        Xe[k] = Xp[k] + d;
-    }
-    ahead(Xe);
+    for (int k = 0; k < 3; k++) Xp[k] += (uint64_t)float_to_fx(dpre[k]);
     field(Xp, E, B);
     B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
     iB = rsqrtf(B2);
