@@ -34,7 +34,7 @@ def setup(kind, steps, n=8192, seed=5):
         cfg = wl.config_modesum(nptl=n, steps=steps)
         dom.xmax = dom.ymax = dom.zmax = 1.0
         dom.tmax = steps * cfg["dt"] + 0.5 * cfg["dt"]
-        # 512 modes: the mode table alone takes 22 KB of shared memory
+        # 512 modes: the mode table alone takes 20 KB of shared memory
         nm, kmax = (512, 64) if kind == "modesum512" else (128, 16)
         modes = wl.kolmogorov_modes(nm, 1, kmax, 1.0, seed, va=0.1)
         tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=1.0)
