@@ -50,6 +50,14 @@ __device__ __forceinline__ void cell_of(uint64_t X, int n, int& i, float& fr)
     fr = (float)(uint32_t)G * 2.3283064365386963e-10f;  // 2^-32
 }
 
+// 32 bytes from global memory through the read-only path in one load
+__device__ __forceinline__ void ld_node32(const float4* p, float4& a, float4& b)
+{
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+                 : "l"(p));
+}
+
 // The eight corner nodes of the cell a particle last sampled, kept in
 // registers: at a few tenths of a cell per step most evaluations fall in the
 // same cell as the previous one and need no memory traffic at all.
@@ -79,6 +87,12 @@ __device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __r
     const uint32_t base = ix + nx * iy + nxy * iz;
     if (base != cc.key) {
         const float4* p = g + (size_t)base * STRIDE;
+        if (STRIDE == 2) {
+            // one 32-byte load per corner node ({E,0},{B,0}; nodes are 32-byte aligned)
+            const uint32_t off[8] = {0, 1, nx, nx + 1, nxy, nxy + 1, nxy + nx, nxy + nx + 1};
+#pragma unroll
+            for (int k = 0; k < 8; k++) ld_node32(p + (size_t)off[k] * 2, cc.c[2 * k], cc.c[2 * k + 1]);
+        } else
 #pragma unroll
         for (int c = 0; c < STRIDE; c++) {
             cc.c[0 * STRIDE + c] = __ldg(p + c);
