@@ -76,9 +76,12 @@ __device__ __forceinline__ void wirz_f32(const MixField& f, PM& p, float dt, Fie
     float dpre[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) dpre[k] = (h[k] * a1 + hp[k] * a2 + hr[k] * a3) * f.invL[k];
-    uint64_t Xp[3] = {p.X[0], p.X[1], p.X[2]};
+    // The midpoint is only sampled, and the field evaluations read the top 32
+    // bits of a position: a 32-bit fixed-point step is enough there.
+    uint64_t Xp[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) Xp[k] += (uint64_t)float_to_fx(dpre[k]);
+    for (int k = 0; k < 3; k++)
+        Xp[k] = (uint64_t)((uint32_t)(p.X[k] >> 32) + (uint32_t)__float2int_rn(dpre[k] * 4294967296.0f)) << 32;
     field(Xp, E, B);
     B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
     iB = rsqrtf(B2);
