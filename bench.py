@@ -37,7 +37,7 @@ UNIT = "pushes/s"
 # 200 steps: 2.130 GB for 26,214,400 pushes); the headline workload has the
 # same particle density per cell, so its traffic scales with the pushes.
 # Summary: profiles/track_mixed_kernel_pic_256cube_131072ptl.txt
-DRAM_BYTES_PER_PUSH = (2.119457e9 + 10.865920e6) / 26214400.0
+DRAM_BYTES_PER_PUSH = (2.119311e9 + 10.339840e6) / 26214400.0
 
 
 def peaks():
