@@ -19,25 +19,26 @@ __device__ __forceinline__ float fx_to_float(uint64_t d)  // signed fixed-point 
 
 // Box fraction -> signed 64-bit fixed point (fr * 2^64) with 32-bit
 // conversions only (64-bit float-to-integer conversions run on the FP64 pipe,
-// a 64th of the FP32 rate on this part).  |fr| < 0.5: the integer part of
-// |fr| * 2^32 and the 32 bits below it are both exact in FP32 arithmetic.
+// a 64th of the FP32 rate on this part).  |fr| < 0.5: fr * 2^64 = hi * 2^32 +
+// lo with hi = floor(fr * 2^32) and lo = the fraction below it times 2^32,
+// two's complement without a sign branch.
 __device__ __forceinline__ int64_t float_to_fx(float fr)
 {
-    float a = fabsf(fr) * 4294967296.0f;
-    float fh = floorf(a);
-    uint32_t hi = __float2uint_rz(fh);
-    uint32_t lo = __float2uint_rz((a - fh) * 4294967296.0f);
-    uint64_t mag = ((uint64_t)hi << 32) | lo;
-    return fr < 0.0f ? -(int64_t)mag : (int64_t)mag;
+    const float a = fr * 4294967296.0f;
+    const float fh = floorf(a);
+    const uint32_t hi = (uint32_t)__float2int_rz(fh);
+    const uint32_t lo = __float2uint_rz((a - fh) * 4294967296.0f);
+    return (int64_t)(((uint64_t)hi << 32) | lo);
 }
 
-// Adds a displacement (in box fractions) to a position, counting periods.
+// Adds a displacement (in box fractions) to a position, counting periods:
+// the period count takes the carry out of the 64-bit sum, less one for a
+// negative displacement.
 __device__ __forceinline__ void advance(uint64_t& X, int& img, float fr)
 {
-    int64_t d = float_to_fx(fr);
-    uint64_t nx = X + (uint64_t)d;
-    if (d > 0 && nx < X) img++;
-    else if (d < 0 && nx > X) img--;
+    const int64_t d = float_to_fx(fr);
+    const uint64_t nx = X + (uint64_t)d;
+    img += (int)(nx < X) - (int)(d < 0);
     X = nx;
 }
 
