@@ -187,6 +187,9 @@ int tp_last_status(void);             /* 0 = ok; sticky until tp_clear_status() 
 const char *tp_last_error(void);
 void tp_clear_status(void);
 int tp_device_status(void);           /* status bits raised by kernels since the last call (read and cleared) */
+/* Device status bits: 1 a gather index outside the grid, 2 a non-finite
+ * field or state, 4 an adaptive step or reject limit reached, 8 a step size
+ * underflow, 16 a bounded wait of the tensor-core pipeline ran out. */
 
 /* Reference compile-time choices made run-time switches. */
 void tp_set_abc(double A, double B, double C);   /* include/force_free.h:21-26 */
@@ -273,6 +276,12 @@ int tp_mlp_train(long long nsamples, int batch, int epochs, double lr, double wd
 int tp_mlp_eval(int n, const unsigned int *u, float *out6);
 /* Same, through the block-wide evaluation the tracking kernel uses. */
 int tp_mlp_eval_kernel(int n, const unsigned int *u, float *out6);
+/* Polls before a hand-over wait of the tensor-core pipeline (learned field)
+ * gives up; 0 restores the default (about 4 million).  A wait that runs out
+ * sets status bit 16 (see tp_device_status), every other wait of the block then
+ * returns at once, the block writes no particle results, drains its MMAs and
+ * copies and frees its tensor memory.  For tests of that path. */
+int tp_set_wait_limit(unsigned int polls);
 
 /* One 128-row tile of D = A * B^T on the tensor cores (tcgen05.mma, BF16
  * operands given as raw 16-bit patterns, FP32 result): A[128][k], B[n][k],

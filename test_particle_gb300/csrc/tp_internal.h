@@ -37,6 +37,7 @@ struct Ctx {
     // ABC coefficients: compile-time macros in the reference (include/force_free.h:21-26)
     double ffA = 1.0, ffB = 0.81649658092772603, ffC = 0.57735026918962573;
     int interp_corrected = 0, ellint_corrected = 0;
+    unsigned int wait_limit = 0;  // tensor-core pipeline hand-over polls (0: default)
     std::vector<tp_mode> modes;
     double mode_B0 = 1.0;
     long modes_gen = 0;

@@ -97,6 +97,7 @@ struct Pipe {
     uint32_t accf, aready;           // a layer's accumulators complete / A operands written
     uint32_t done;                   // MMA thread: every MMA it issued has completed
     uint32_t tmem;
+    uint32_t lim;                    // polls before a hand-over wait gives up
     int* abort;                      // a bounded wait ran out (or the MMA thread failed)
     int* stop;                       // consumers are finished
     const float* bias;               // shared copy: 4 x 256 hidden biases then 6 output biases
@@ -106,9 +107,9 @@ struct Pipe {
 
 // Bounded wait that also gives up once the block has aborted; a wait that
 // runs out marks the block aborted.
-__device__ __forceinline__ bool wait_or_abort(uint32_t bar, uint32_t parity, int* abort)
+__device__ __forceinline__ bool wait_or_abort(uint32_t bar, uint32_t parity, int* abort, uint32_t lim)
 {
-    for (uint32_t it = 0; it < kWaitLimit; it++) {
+    for (uint32_t it = 0; it < lim; it++) {
         if (tc::mbar_try_wait(bar, parity)) return true;
         if ((it & 63u) == 63u && *(volatile int*)abort) return false;
     }
@@ -131,7 +132,7 @@ __device__ __noinline__ void loader(const Pipe& pp, const unsigned char* wpack)
         const uint32_t s = u % kStages, use = u / kStages;
         if (use > 0) {
             bool ok = false;
-            for (uint32_t it = 0; it < kWaitLimit && !ok; it++) {
+            for (uint32_t it = 0; it < pp.lim && !ok; it++) {
                 ok = tc::mbar_try_wait(pp.empty + 8 * s, (use - 1) & 1);
                 if (!ok && (it & 63u) == 63u && (*(volatile int*)pp.abort || *(volatile int*)pp.stop)) break;
             }
@@ -168,7 +169,7 @@ __device__ __noinline__ void mma_issuer(const Pipe& pp, int* status)
     for (int t = 0; t < kTiles; t++) adesc[t] = tc::desc_sw128(tc::smem_addr(pp.a[t]));
     while (ok) {
         for (int l = 0; ok && l < kLayers; l++) {
-            ok = wait_or_abort(pp.aready, nready & 1, pp.abort);
+            ok = wait_or_abort(pp.aready, nready & 1, pp.abort, pp.lim);
             nready++;
             if (ok && *(volatile int*)pp.stop) {
                 stopped = true;
@@ -182,7 +183,8 @@ __device__ __noinline__ void mma_issuer(const Pipe& pp, int* status)
             const uint32_t c_end = next_use + (uint32_t)(layer_first_chunk(l + 1) - layer_first_chunk(l));
             for (uint32_t c = next_use; ok && c < c_end; c += width) {
                 for (uint32_t w = 0; w < width && ok; w++)
-                    ok = wait_or_abort(pp.full + 8 * ((c + w) % kStages), ((c + w) / kStages) & 1, pp.abort);
+                    ok = wait_or_abort(pp.full + 8 * ((c + w) % kStages), ((c + w) / kStages) & 1, pp.abort,
+                                       pp.lim);
                 if (!ok) break;
                 tc::tc_fence_after();
                 const Chunk ch = chunk_of((int)(c % kChunks));
@@ -260,7 +262,7 @@ __device__ __noinline__ void field_tile(const Model& md, const Pipe& pp, Cons& c
     tc::tc_fence_before();
     tc::mbar_arrive(aready);
     for (int l = 0; l < kLayers; l++) {
-        wait_or_abort(accf, cs.nacc & 1, pp.abort);
+        wait_or_abort(accf, cs.nacc & 1, pp.abort, pp.lim);
         cs.nacc++;
         tc::tc_fence_after();
         if (l < kLayers - 1) {
@@ -318,7 +320,7 @@ struct SmemStatic {
     int stop;
 };
 
-__device__ void pipe_setup(Pipe& pp, SmemStatic& st, unsigned char* dyn, const Model& md)
+__device__ void pipe_setup(Pipe& pp, SmemStatic& st, unsigned char* dyn, const Model& md, uint32_t wait_limit)
 {
     const int tid = threadIdx.x;
     const uint32_t raw = tc::smem_addr(dyn);
@@ -336,6 +338,7 @@ __device__ void pipe_setup(Pipe& pp, SmemStatic& st, unsigned char* dyn, const M
     pp.accf = tc::smem_addr(&st.bars[2 * kStages]);
     pp.aready = tc::smem_addr(&st.bars[2 * kStages + 1]);
     pp.done = tc::smem_addr(&st.bars[2 * kStages + 2]);
+    pp.lim = wait_limit ? wait_limit : kWaitLimit;
     pp.abort = &st.abort;
     pp.stop = &st.stop;
     pp.bias = st.bias;
@@ -408,7 +411,8 @@ __device__ __forceinline__ void consumers_diff_sum(const double sg[8], double* r
 // their frozen position and discard the result.  Threads 0..kB-1 own one
 // particle each; then the MMA warp and the loader warps.
 __global__ void __launch_bounds__(kThreads, 1) track_surrogate_kernel(mixed::MixField f, Model md,
-                                                                       TrackBufs b, TrackParams q)
+                                                                       TrackBufs b, TrackParams q,
+                                                                       uint32_t wait_limit)
 {
     using namespace mixed;
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
@@ -416,7 +420,7 @@ __global__ void __launch_bounds__(kThreads, 1) track_surrogate_kernel(mixed::Mix
     __shared__ double red[(kB / 32) * 8];
     __shared__ unsigned int hist[kSurrSmemBins];
     Pipe pp;
-    pipe_setup(pp, st, smem_dyn, md);
+    pipe_setup(pp, st, smem_dyn, md, wait_limit);
     if (threadIdx.x >= kB) {
         if (threadIdx.x / 32 >= kLoaderWarp0) loader(pp, md.wpack);
         else if (threadIdx.x == kMmaWarp * 32) mma_issuer(pp, b.status);
@@ -566,12 +570,13 @@ __global__ void __launch_bounds__(kThreads, 1) track_surrogate_kernel(mixed::Mix
 
 // Model field at n positions through the in-kernel (per-block) evaluation path.
 __global__ void __launch_bounds__(kThreads, 1) field_eval_kernel(Model md, const uint32_t* __restrict__ U,
-                                                                  int n, float* __restrict__ out, int* status)
+                                                                  int n, float* __restrict__ out, int* status,
+                                                                  uint32_t wait_limit)
 {
     extern __shared__ __align__(1024) unsigned char smem_dyn[];
     __shared__ SmemStatic st;
     Pipe pp;
-    pipe_setup(pp, st, smem_dyn, md);
+    pipe_setup(pp, st, smem_dyn, md, wait_limit);
     if (threadIdx.x >= kB) {
         if (threadIdx.x / 32 >= kLoaderWarp0) loader(pp, md.wpack);
         else if (threadIdx.x == kMmaWarp * 32) mma_issuer(pp, status);
@@ -627,7 +632,7 @@ cudaError_t launch_track_surrogate(const mixed::MixField& f, const Model& md, co
     cudaError_t e = cudaFuncSetAttribute(track_surrogate_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDyn);
     if (e != cudaSuccess) return e;
-    track_surrogate_kernel<<<grid, kThreads, kSmemDyn, s>>>(f, md, b, q);
+    track_surrogate_kernel<<<grid, kThreads, kSmemDyn, s>>>(f, md, b, q, g.wait_limit);
     return cudaGetLastError();
 }
 
@@ -635,6 +640,15 @@ cudaError_t launch_track_surrogate(const mixed::MixField& f, const Model& md, co
 }  // namespace tp
 
 using namespace tp;
+
+// Polls before a hand-over wait of the tensor-core pipeline gives up (0: the
+// default, about 4 million); a small value makes the waits run out, for tests
+// of the timeout path.
+extern "C" int tp_set_wait_limit(unsigned int polls)
+{
+    g.wait_limit = polls;
+    return 0;
+}
 
 // Model field at n positions evaluated by the block-wide kernel path used in tracking.
 extern "C" int tp_mlp_eval_kernel(int n, const unsigned int* u, float* out6)
@@ -653,7 +667,7 @@ extern "C" int tp_mlp_eval_kernel(int n, const unsigned int* u, float* out6)
     if (ok) {
         int grid = (n + mlp::kB - 1) / mlp::kB;
         if (grid > g.num_sms) grid = g.num_sms;
-        mlp::field_eval_kernel<<<grid, mlp::kThreads, mlp::kSmemDyn, s>>>(md, dU, n, dO, g.d_status);
+        mlp::field_eval_kernel<<<grid, mlp::kThreads, mlp::kSmemDyn, s>>>(md, dU, n, dO, g.d_status, g.wait_limit);
         ok = cuda_ok(cudaGetLastError(), "field eval");
     }
     if (ok) {

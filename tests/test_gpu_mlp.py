@@ -108,6 +108,38 @@ def test_surrogate_tracking_runs_and_tracks_the_exact_field():
     assert tp.device_status() == 0
 
 
+def test_stalled_pipeline_is_reported_and_the_context_survives():
+    """The bounded hand-over waits of the tensor-core pipeline: with a limit of
+    one poll they run out, the tracking kernel raises status bit 16 and stops
+    its blocks cleanly; with the default limit restored the same run gives the
+    ordinary results on the same context."""
+    modes = small_modes()
+    dom = tp.Domain()
+    dom.xmax = dom.ymax = dom.zmax = 1.0
+    steps = 50
+    dt = wl.gyro_dt(0.7, 1.0)
+    dom.tmax = steps * dt + 0.5 * dt
+    tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=1.0)
+    tp.mlp_init(lattice_freq(5), seed=4)
+    tp.set_spectrum(200, 1e-3, 1e2)
+    p0 = wl.shell_particles(2048, 0.7, (0, 0, 0), (1, 1, 1), 9)
+    tp.device_status()
+    ref = tp.track(p0, dt, 1, 200, precision=tp.PREC_SURROGATE)
+    assert tp.device_status() == 0
+    tp.check(tp.lib().tp_set_wait_limit(1), "wait limit")
+    try:
+        tp.track(p0, dt, 1, 200, precision=tp.PREC_SURROGATE)
+        status = tp.device_status()
+    finally:
+        tp.check(tp.lib().tp_set_wait_limit(0), "wait limit")
+    assert status & 16, status
+    again = tp.track(p0, dt, 1, 200, precision=tp.PREC_SURROGATE)
+    assert tp.device_status() == 0
+    for c in ("x", "y", "z", "ux", "uy", "uz"):
+        assert np.array_equal(again["ptl"][c], ref["ptl"][c]), c
+    assert np.array_equal(again["espect"], ref["espect"])
+
+
 def test_tensor_core_inference_matches_fp64_forward():
     """The in-kernel evaluation (tcgen05.mma chain, BF16 weights and
     activations, FP32 accumulation in tensor memory) against the FP64 forward
