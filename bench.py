@@ -474,6 +474,17 @@ def main():
     e1 = diag["espect"][-1] / max(1.0, diag["espect"][-1].sum())
     e2 = d64["espect"][-1] / max(1.0, d64["espect"][-1].sum())
     spec_l1 = float(np.abs(e1 - e2).sum())
+    # per output frame: the L1 distance of the two spectra, and the distance
+    # two independent ensembles of this size drawn from the FP64 spectrum would
+    # show (sum over bins of sqrt(4 p (1 - p) / (pi N))): while the paths still
+    # follow the same trajectories the first is far below the second, once
+    # chaos has decorrelated them it sits at it
+    frames_l1, frames_floor = [], []
+    for fa, fb in zip(diag["espect"], d64["espect"]):
+        na, nb = max(1.0, fa.sum()), max(1.0, fb.sum())
+        frames_l1.append(float(np.abs(fa / na - fb / nb).sum()))
+        q = fb / nb
+        frames_floor.append(float(np.sqrt(4 * q * (1 - q) / (np.pi * nb)).sum()))
     dc_rel = np.abs(diag["dsum"][:, -1] - d64["dsum"][:, -1]) / np.maximum(np.abs(d64["dsum"][:, -1]), 1e-300)
     sess.close()
 
@@ -526,6 +537,9 @@ def main():
             "fp64": {"value": fp64_value * world, "unit": UNIT,
                      "mixed_over_fp64": value / (fp64_value * world),
                      "spectrum_l1_mixed_vs_fp64": spec_l1,
+                     "spectrum_l1_per_frame": frames_l1,
+                     "spectrum_l1_sampling_floor_per_frame": frames_floor,
+                     "frame_steps": [int(cfg["steps"] // nt_out * k) for k in range(nt_out)],
                      "diffusion_rel_err_mixed_vs_fp64_final": [float(v) for v in dc_rel],
                      "diffusion_order": ["drr", "dxx", "dyy", "dzz", "dpp", "duu", "daa", "dee"]},
             }
