@@ -471,6 +471,14 @@ def main():
         f64.append(sess.track(dt, nt_out, nbins, tp.PREC_FP64).kernel_ms)
     fp64_value = pushes / (float(np.median(f64)) / 1e3)
     d64 = sess.fetch(nt_out, nbins, info.nsdc)
+    # the FP64 path again from the initial state rounded to FP32: how far two
+    # FP64 runs drift apart from a difference of one FP32 rounding (chaos)
+    p0r = p0.copy()
+    for c in ("x", "y", "z", "ux", "uy", "uz"):
+        p0r[c] = p0r[c].astype(np.float32).astype(np.float64)
+    sess.load(p0r)
+    sess.track(dt, nt_out, nbins, tp.PREC_FP64)
+    d64r = sess.fetch(nt_out, nbins, info.nsdc)
     e1 = diag["espect"][-1] / max(1.0, diag["espect"][-1].sum())
     e2 = d64["espect"][-1] / max(1.0, d64["espect"][-1].sum())
     spec_l1 = float(np.abs(e1 - e2).sum())
@@ -479,12 +487,17 @@ def main():
     # show (sum over bins of sqrt(4 p (1 - p) / (pi N))): while the paths still
     # follow the same trajectories the first is far below the second, once
     # chaos has decorrelated them it sits at it
-    frames_l1, frames_floor = [], []
-    for fa, fb in zip(diag["espect"], d64["espect"]):
-        na, nb = max(1.0, fa.sum()), max(1.0, fb.sum())
-        frames_l1.append(float(np.abs(fa / na - fb / nb).sum()))
+    def l1(fa, fb):
+        return float(np.abs(fa / max(1.0, fa.sum()) - fb / max(1.0, fb.sum())).sum())
+
+    frames_l1 = [l1(fa, fb) for fa, fb in zip(diag["espect"], d64["espect"])]
+    frames_chaos = [l1(fa, fb) for fa, fb in zip(d64r["espect"], d64["espect"])]
+    frames_floor = []
+    for fb in d64["espect"]:
+        nb = max(1.0, fb.sum())
         q = fb / nb
         frames_floor.append(float(np.sqrt(4 * q * (1 - q) / (np.pi * nb)).sum()))
+    dc_chaos = np.abs(d64r["dsum"][:, -1] - d64["dsum"][:, -1]) / np.maximum(np.abs(d64["dsum"][:, -1]), 1e-300)
     dc_rel = np.abs(diag["dsum"][:, -1] - d64["dsum"][:, -1]) / np.maximum(np.abs(d64["dsum"][:, -1]), 1e-300)
     sess.close()
 
@@ -538,7 +551,9 @@ def main():
                      "mixed_over_fp64": value / (fp64_value * world),
                      "spectrum_l1_mixed_vs_fp64": spec_l1,
                      "spectrum_l1_per_frame": frames_l1,
+                     "spectrum_l1_fp64_from_fp32_rounded_start_per_frame": frames_chaos,
                      "spectrum_l1_sampling_floor_per_frame": frames_floor,
+                     "diffusion_rel_err_fp64_from_fp32_rounded_start_final": [float(v) for v in dc_chaos],
                      "frame_steps": [int(cfg["steps"] // nt_out * k) for k in range(nt_out)],
                      "diffusion_rel_err_mixed_vs_fp64_final": [float(v) for v in dc_rel],
                      "diffusion_order": ["drr", "dxx", "dyy", "dzz", "dpp", "duu", "daa", "dee"]},
