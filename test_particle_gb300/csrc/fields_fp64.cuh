@@ -349,8 +349,14 @@ __device__ __forceinline__ void emf64(const DevField& f, double x, double y, dou
             double B[3], E[3];
             wlcs c = f.cfg[i];
             if (f.iBessel == 0) {
-                wl_wire_static(c, x, y, z, B);
-                Bx += B[0]; By += B[1]; Bz += B[2];
+                // A wire without current adds exact zeros (its B is the
+                // current times finite factors, the radius clamped at 0.1),
+                // which leave the sums bit for bit as they are: skip its
+                // square root, arc cosine, sine and cosine.
+                if (c.cur_wr != 0.0) {
+                    wl_wire_static(c, x, y, z, B);
+                    Bx += B[0]; By += B[1]; Bz += B[2];
+                }
             } else {
                 wl_wire_bessel(c, x, y, z, t, B, E);
                 Bx += B[0]; Ex += E[0];
