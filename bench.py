@@ -209,10 +209,22 @@ def profile_case(prec):
     gridded field (256^3, 0.5 GB interleaved, larger than L2; 131072
     particles, 200 steps) for mixed / fp64 / fp64fast; the 512-mode field
     with an untrained learned model (the kernel's work does not depend on the
-    weights; 155648 particles = 2 x 304 blocks of 256, 20 steps) for surrogate."""
+    weights; 155648 particles = 2 x 304 blocks of 256, 20 steps) for surrogate;
+    the mixed kernel on the 512-mode field (155648 particles, 20 steps) for
+    modesum and on the ABC field (65536 particles, 1000 steps) for abc."""
     import test_particle_gb300 as tp
     import test_particle_gb300.workloads as wl
-    if prec == "surrogate":
+    if prec == "abc":
+        tp.check(tp.lib().tp_init(0), "tp_init")
+        cfg = wl.config_abc(steps=1000)
+        dom = tp.Domain()
+        dom.xmax = dom.ymax = dom.zmax = 1.0
+        dom.tmax = cfg["steps"] * cfg["dt"] + 0.5 * cfg["dt"]
+        tp.configure(system_type=tp.SYS_FORCEFREE, dom=dom, abc=(1.0, 1.0, 1.0), B0=1.0,
+                     lambda0=2 * np.pi)
+        tp.set_spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
+        p0 = wl.shell_particles(cfg["nptl"], cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"])
+    elif prec in ("surrogate", "modesum"):
         tp.check(tp.lib().tp_init(0), "tp_init")
         cfg = wl.config_modesum(nptl=155648, steps=20)
         dom = tp.Domain()
@@ -222,16 +234,17 @@ def profile_case(prec):
                                     va=cfg["va"])
         tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=cfg["B0"])
         tp.set_spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
-        amp = np.linalg.norm(modes["amp_b"], axis=1)
-        tp.mlp_init(modes["n"][np.argsort(-amp)[:64]], seed=3)
-        tp.mlp_set_output_norm(np.array([0, 0, 1, 0, 0, 0]), np.ones(6))
+        if prec == "surrogate":
+            amp = np.linalg.norm(modes["amp_b"], axis=1)
+            tp.mlp_init(modes["n"][np.argsort(-amp)[:64]], seed=3)
+            tp.mlp_set_output_norm(np.array([0, 0, 1, 0, 0, 0]), np.ones(6))
         p0 = wl.shell_particles(cfg["nptl"], cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"])
     else:
         cfg = wl.config_grid(nptl=131072, steps=200, n=256)
         dom, grd, p0, _, _ = setup_grid(tp, wl, cfg, 0)
     sess = tp.Session(cfg["nptl"])
     code = {"mixed": tp.PREC_MIXED, "fp64": tp.PREC_FP64, "fp64fast": tp.PREC_FP64_FAST,
-            "surrogate": tp.PREC_SURROGATE}[prec]
+            "surrogate": tp.PREC_SURROGATE, "modesum": tp.PREC_MIXED, "abc": tp.PREC_MIXED}[prec]
     sess.load(p0)
     sess.track(cfg["dt"], 2, cfg["nbins"], code)
     sess.load(p0)
@@ -415,10 +428,11 @@ def main():
     ap.add_argument("--acc-steps", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=4)
     ap.add_argument("--cpu-bs", action="store_true")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "fp64fast", "surrogate"], default=None,
+    ap.add_argument("--profile", choices=["mixed", "fp64", "fp64fast", "surrogate", "modesum", "abc"],
+                    default=None,
                     help="one tracking launch of a small case for a profiler capture (gridded "
-                         "field 256^3, 131072 particles, 200 steps; surrogate: 512-mode field, "
-                         "155648 particles, 20 steps)")
+                         "field 256^3, 131072 particles, 200 steps; surrogate and modesum: 512-mode "
+                         "field, 155648 particles, 20 steps; abc: 65536 particles, 1000 steps)")
     args = ap.parse_args()
     if args.profile:
         profile_case(args.profile)
