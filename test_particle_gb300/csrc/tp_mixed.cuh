@@ -50,6 +50,31 @@ __device__ __forceinline__ void cell_of(uint64_t X, int n, int& i, float& fr)
     fr = (float)(uint32_t)G * 2.3283064365386963e-10f;  // 2^-32
 }
 
+// Packed FP32 pairs (f32x2): two lanes of one 64-bit register, each rounded as
+// the scalar operation would be.
+__device__ __forceinline__ uint64_t pack_f2(float a, float b)
+{
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void unpack_f2(uint64_t v, float& a, float& b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t mul_f2(uint64_t a, uint64_t b)
+{
+    uint64_t r;
+    asm("mul.rn.ftz.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t fma_f2(uint64_t a, uint64_t b, uint64_t c)
+{
+    uint64_t r;
+    asm("fma.rn.ftz.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 // 32 bytes from global memory through the read-only path in one load
 __device__ __forceinline__ void ld_node32(const float4* p, float4& a, float4& b)
 {
@@ -112,14 +137,22 @@ __device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __r
     const float w[8] = {gx * a00, fx * a00, gx * a10, fx * a10, gx * a01, fx * a01, gx * a11, fx * a11};
 #pragma unroll
     for (int c = 0; c < STRIDE; c++) {
-        float4 r = make_float4(w[0] * cc.c[c].x, w[0] * cc.c[c].y, w[0] * cc.c[c].z, 0.f);
+        // packed FP32 pairs (x, y) and (z, pad): the same products and sums,
+        // in the same order, with half the instructions
+        uint64_t wp = pack_f2(w[0], w[0]);
+        uint64_t rxy = mul_f2(wp, pack_f2(cc.c[c].x, cc.c[c].y));
+        uint64_t rzw = mul_f2(wp, pack_f2(cc.c[c].z, cc.c[c].w));
 #pragma unroll
         for (int k = 1; k < 8; k++) {
             const float4 v = cc.c[k * STRIDE + c];
-            r.x = fmaf(w[k], v.x, r.x);
-            r.y = fmaf(w[k], v.y, r.y);
-            r.z = fmaf(w[k], v.z, r.z);
+            wp = pack_f2(w[k], w[k]);
+            rxy = fma_f2(wp, pack_f2(v.x, v.y), rxy);
+            rzw = fma_f2(wp, pack_f2(v.z, v.w), rzw);
         }
+        float4 r;
+        unpack_f2(rxy, r.x, r.y);
+        unpack_f2(rzw, r.z, r.w);
+        r.w = 0.f;
         out[c] = r;
     }
 }
