@@ -78,7 +78,7 @@ __device__ __forceinline__ uint64_t fma_f2(uint64_t a, uint64_t b, uint64_t c)
 // 32 bytes from global memory through the read-only path in one load
 __device__ __forceinline__ void ld_node32(const float4* p, float4& a, float4& b)
 {
-    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
                  : "l"(p));
 }
@@ -112,7 +112,7 @@ __device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __r
     const uint32_t base = ix + nx * iy + nxy * iz;
     if (base != cc.key) {
         const float4* p = g + (size_t)base * STRIDE;
-        if (STRIDE == 2) {
+        if constexpr (STRIDE == 2) {
             // one 32-byte load per corner node ({E,0},{B,0}; nodes are 32-byte aligned)
             const uint32_t off[8] = {0, 1, nx, nx + 1, nxy, nxy + 1, nxy + nx, nxy + nx + 1};
 #pragma unroll
