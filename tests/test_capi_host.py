@@ -124,6 +124,52 @@ def test_scalar_helpers(lib):
     assert (cx.value, cy.value, cz.value) == (0.0, 0.0, 1.0)
 
 
+def test_gather_particle_spectra(lib):
+    """src/tracking.c:475-493: the per-thread rows add into the spectra; the
+    escape spectra only with open boundaries (bc_flag 1)."""
+    rng = np.random.default_rng(5)
+    nth, nb, nt = 3, 7, 4
+    ep = rng.integers(0, 9, (nth, nt * nb)).astype(np.float64)
+    eep = rng.integers(0, 9, (nth, nt * nb)).astype(np.float64)
+    bc = C.c_int.in_dll(lib, "bc_flag")
+    old = bc.value
+    try:
+        for flag in (1, 0, 2):
+            bc.value = flag
+            esp, ese = np.full(nt * nb, 0.5), np.full(nt * nb, 0.25)
+            lib.gather_particle_spectra_openmp(C.c_int(nth), C.c_int(nb), C.c_int(nt),
+                                               esp.ctypes.data_as(C.c_void_p),
+                                               ep.ctypes.data_as(C.c_void_p),
+                                               ese.ctypes.data_as(C.c_void_p),
+                                               eep.ctypes.data_as(C.c_void_p))
+            assert np.array_equal(esp, 0.5 + ep.sum(0))
+            assert np.array_equal(ese, 0.25 + eep.sum(0) if flag == 1 else np.full(nt * nb, 0.25))
+    finally:
+        bc.value = old
+
+
+def test_diff_coeff_file_format(lib, tmp_path):
+    """The single-rank collect_diff_coeffs writes the reference's table
+    (src/diagnostics.c:723-782): a header line, then per sample the eight
+    sums as %10.4e and the remaining particle count."""
+    ns = 3
+    cols = [np.arange(ns) * (c + 1) * 1.25e-3 for c in range(8)]
+    rem = np.array([10, 9, 7], dtype=np.int32)
+    fname = str(tmp_path / "dc.dat").encode()
+    lib.collect_diff_coeffs(C.c_int(0), C.c_int(ns), *[c.ctypes.data_as(C.c_void_p) for c in cols],
+                            C.c_char_p(fname), rem.ctypes.data_as(C.c_void_p))
+    lines = (tmp_path / "dc.dat").read_text().splitlines()
+    assert lines[0] == "drr        dxx        dyy        dzz        dpp        duu        daa        dee        nptl"
+    for i in range(ns):
+        want = " ".join("%10.4e" % c[i] for c in cols) + " %d" % rem[i]
+        assert lines[1 + i] == want
+    # rank > 0 writes nothing
+    lib.collect_diff_coeffs(C.c_int(1), C.c_int(ns), *[c.ctypes.data_as(C.c_void_p) for c in cols],
+                            C.c_char_p(str(tmp_path / "none.dat").encode()),
+                            rem.ctypes.data_as(C.c_void_p))
+    assert not (tmp_path / "none.dat").exists()
+
+
 def test_no_gpu_is_an_error_not_a_fallback(lib):
     """Without a device the compute entry points fail loudly."""
     import test_particle_gb300 as tp
