@@ -119,24 +119,38 @@ bool build_mixfield(int stype, mixed::MixField& mf, int* nmodes_out)
         mf.eb = (const float4*)g.s_mix_eb.ptr;
     } else if (stype == TP_SYS_MODESUM) {
         int nm = (int)g.modes.size();
-        if (sizeof(mixed::ModeF) * (size_t)nm > 200 * 1024) {
-            set_error(10, "at most %d plane-wave modes fit in shared memory", (int)(200 * 1024 / sizeof(mixed::ModeF)));
+        int npair = (nm + 1) / 2;
+        if (sizeof(mixed::ModePair) * (size_t)npair > 200 * 1024) {
+            set_error(10, "at most %d plane-wave modes fit in shared memory",
+                      (int)(200 * 1024 / sizeof(mixed::ModePair)) * 2);
             return false;
         }
-        std::vector<mixed::ModeF> mfv(nm);
+        std::vector<mixed::ModePair> mfv(npair);
+        memset(mfv.data(), 0, sizeof(mixed::ModePair) * npair);
         for (int m = 0; m < nm; m++) {
             const tp_mode& md = g.modes[m];
-            mixed::ModeF& o = mfv[m];
+            mixed::ModePair& o = mfv[m / 2];
+            const int h = m & 1;
+            // round(phase / 2pi * 2^32) mod 2^32 is kept in the mode's pad word
+            o.nph[h] = make_int4(md.n[0], md.n[1], md.n[2], md.pad);
+            const float v[6] = {(float)md.amp_b[0], (float)md.amp_b[1], (float)md.amp_b[2],
+                                (float)md.amp_e[0], (float)md.amp_e[1], (float)md.amp_e[2]};
+            unsigned long long pk[3];  // (b0,b1) (b2,e0) (e1,e2), first of a pair in the low half
             for (int k = 0; k < 3; k++) {
-                o.n[k] = md.n[k];
-                o.b[k] = (float)md.amp_b[k];
-                o.e[k] = (float)md.amp_e[k];
+                uint32_t lo, hi;
+                memcpy(&lo, &v[2 * k], 4);
+                memcpy(&hi, &v[2 * k + 1], 4);
+                pk[k] = (unsigned long long)lo | ((unsigned long long)hi << 32);
             }
-            o.ph = (uint32_t)md.pad;  // round(phase / 2pi * 2^32) mod 2^32
+            if (h == 0) {
+                o.amp[0].x = pk[0]; o.amp[0].y = pk[1]; o.amp[1].x = pk[2];
+            } else {
+                o.amp[1].y = pk[0]; o.amp[2].x = pk[1]; o.amp[2].y = pk[2];
+            }
         }
-        mixed::ModeF* d = (mixed::ModeF*)g.s_mix_modes.get(sizeof(mixed::ModeF) * (nm > 0 ? nm : 1));
+        mixed::ModePair* d = (mixed::ModePair*)g.s_mix_modes.get(sizeof(mixed::ModePair) * (npair > 0 ? npair : 1));
         if (!d) return false;
-        if (nm) cudaMemcpyAsync(d, mfv.data(), sizeof(mixed::ModeF) * nm, cudaMemcpyHostToDevice, s);
+        if (nm) cudaMemcpyAsync(d, mfv.data(), sizeof(mixed::ModePair) * npair, cudaMemcpyHostToDevice, s);
         cudaStreamSynchronize(s);
         mf.nmodes = nm;
         mf.modes = d;

@@ -5,13 +5,14 @@
 namespace tp {
 namespace mixed {
 
-// One plane-wave mode in FP32 with its phase offset in 32-bit fixed point
-// (revolutions * 2^32).
-struct ModeF {
-    int n[3];
-    uint32_t ph;
-    float b[3];
-    float e[3];
+// Two plane-wave modes A, B in FP32, 80 bytes read as five 16-byte loads:
+// per mode the lattice vector n and the phase offset in 32-bit fixed point
+// (revolutions * 2^32), then the amplitudes as packed FP32 pairs in the order
+// (bA0,bA1) (bA2,eA0) | (eA1,eA2) (bB0,bB1) | (bB2,eB0) (eB1,eB2).  An odd
+// mode count is padded with a zero-amplitude mode.
+struct alignas(16) ModePair {
+    int4 nph[2];
+    ulonglong2 amp[3];
 };
 
 struct MixField {
@@ -33,7 +34,7 @@ struct MixField {
     const float4* vgrid;
     // plane-wave mode sum, B = mB0 z + sum
     int nmodes;
-    const ModeF* modes;
+    const ModePair* modes;   // (nmodes + 1) / 2 records
     float mB0;
 };
 
@@ -165,7 +166,7 @@ struct FieldCache {
 
 template <int SYS>
 __device__ __forceinline__ void field_mixed(const MixField& f, const uint64_t X[3], float E[3],
-                                            float B[3], const ModeF* smodes, FieldCache& fc)
+                                            float B[3], const ModePair* smodes, FieldCache& fc)
 {
     E[0] = E[1] = E[2] = 0.f;
     if (SYS == TP_SYS_TEST) {
@@ -199,17 +200,26 @@ __device__ __forceinline__ void field_mixed(const MixField& f, const uint64_t X[
     } else if (SYS == TP_SYS_MODESUM) {
         const uint32_t X32 = (uint32_t)(X[0] >> 32), Y32 = (uint32_t)(X[1] >> 32),
                        Z32 = (uint32_t)(X[2] >> 32);
-        float b0 = 0.f, b1 = 0.f, b2 = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f;
-#pragma unroll 4
-        for (int m = 0; m < f.nmodes; m++) {
-            const ModeF& md = smodes[m];
-            uint32_t ph = (uint32_t)md.n[0] * X32 + (uint32_t)md.n[1] * Y32 + (uint32_t)md.n[2] * Z32 + md.ph;
-            float c = __cosf(rev_to_rad(ph));
-            b0 = fmaf(md.b[0], c, b0); b1 = fmaf(md.b[1], c, b1); b2 = fmaf(md.b[2], c, b2);
-            e0 = fmaf(md.e[0], c, e0); e1 = fmaf(md.e[1], c, e1); e2 = fmaf(md.e[2], c, e2);
+        // accumulators (b0,b1) (b2,e0) (e1,e2); each lane sums the modes in
+        // table order with one FMA per mode, as a scalar loop would
+        uint64_t s01 = 0, s23 = 0, s45 = 0;
+        const int npairs = (f.nmodes + 1) >> 1;
+#pragma unroll 2
+        for (int q = 0; q < npairs; q++) {
+            const int4 na = smodes[q].nph[0], nb = smodes[q].nph[1];
+            const ulonglong2 w0 = smodes[q].amp[0], w1 = smodes[q].amp[1], w2 = smodes[q].amp[2];
+            const uint32_t pa = (uint32_t)na.x * X32 + (uint32_t)na.y * Y32 + (uint32_t)na.z * Z32 + (uint32_t)na.w;
+            const uint32_t pb = (uint32_t)nb.x * X32 + (uint32_t)nb.y * Y32 + (uint32_t)nb.z * Z32 + (uint32_t)nb.w;
+            const float ca = __cosf(rev_to_rad(pa)), cb = __cosf(rev_to_rad(pb));
+            const uint64_t cca = pack_f2(ca, ca), ccb = pack_f2(cb, cb);
+            s01 = fma_f2(w0.x, cca, s01); s23 = fma_f2(w0.y, cca, s23); s45 = fma_f2(w1.x, cca, s45);
+            s01 = fma_f2(w1.y, ccb, s01); s23 = fma_f2(w2.x, ccb, s23); s45 = fma_f2(w2.y, ccb, s45);
         }
-        B[0] = b0; B[1] = b1; B[2] = f.mB0 + b2;
-        E[0] = e0; E[1] = e1; E[2] = e2;
+        float b2;
+        unpack_f2(s01, B[0], B[1]);
+        unpack_f2(s23, b2, E[0]);
+        unpack_f2(s45, E[1], E[2]);
+        B[2] = f.mB0 + b2;
     }
 }
 

@@ -22,7 +22,7 @@ namespace mixed {
 // pitch-angle cosine of u against the local field, FP32 field, returned in double
 template <int SYS>
 __device__ __forceinline__ double pitch_mu(const MixField& f, const uint64_t X[3], const float u[3],
-                                           const ModeF* smodes, FieldCache& fc)
+                                           const ModePair* smodes, FieldCache& fc)
 {
     float E[3], B[3];
     field_mixed<SYS>(f, X, E, B, smodes, fc);
@@ -49,9 +49,9 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
     __shared__ double red[(kBlock / 32) * 8];
     __shared__ unsigned int hist[kMaxSmemBins];
     __shared__ double dg[DG_ROWS][kBlock];
-    extern __shared__ ModeF smodes[];
+    extern __shared__ ModePair smodes[];
     if (SYS == TP_SYS_MODESUM) {
-        for (int m = threadIdx.x; m < f.nmodes; m += blockDim.x) smodes[m] = f.modes[m];
+        for (int m = threadIdx.x; m < (f.nmodes + 1) / 2; m += blockDim.x) smodes[m] = f.modes[m];
         __syncthreads();
     }
     const int tx = threadIdx.x;
@@ -198,7 +198,7 @@ template <int SYS>
 static cudaError_t launch_sys(const MixField& f, const TrackBufs& b, const TrackParams& q, int grid,
                               cudaStream_t s)
 {
-    size_t smem = SYS == TP_SYS_MODESUM ? sizeof(ModeF) * (size_t)f.nmodes : 0;
+    size_t smem = SYS == TP_SYS_MODESUM ? sizeof(ModePair) * (size_t)((f.nmodes + 1) / 2) : 0;
     if (smem > 0) {  // static plus dynamic shared memory may pass the 48 KB default
         cudaError_t e = cudaFuncSetAttribute(track_mixed_kernel<SYS>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -223,7 +223,7 @@ cudaError_t launch_track(const MixField& f, const TrackBufs& b, const TrackParam
 int track_max_blocks_per_sm(int system_type, int nmodes)
 {
     int nb = 0;
-    size_t smem = system_type == TP_SYS_MODESUM ? sizeof(ModeF) * (size_t)nmodes : 0;
+    size_t smem = system_type == TP_SYS_MODESUM ? sizeof(ModePair) * (size_t)((nmodes + 1) / 2) : 0;
     cudaError_t e = cudaErrorInvalidValue;
     switch (system_type) {
     case TP_SYS_TEST: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, track_mixed_kernel<TP_SYS_TEST>, kBlock, 0); break;
