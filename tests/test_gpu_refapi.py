@@ -10,7 +10,10 @@ run call (tp_track_host) and the golden runs of the reference build:
   (src/tracking.c:297-375, 475-493) with the particles split between two
   thread slots, the way the reference's `omp for` splits them;
 - particle_tracking_single_step_openmp (src/tracking.c:376-470) driven step by
-  step by the loop of src/tracking.c:313-373, one particle at a time.
+  step by the loop of src/tracking.c:313-373, one particle at a time;
+- particle_tracking_hybrid (src/tracking.c:659-699), the caller's entry point,
+  with the fixed step and with the adaptive stepper, and the spectrum files it
+  writes.
 
 Cases from the golden runs: 0 (uniform test field), 3 (PIC grids), 4 (MHD
 grids) and 5 (force-free field with open boundaries, 44 particles escape).
@@ -27,6 +30,8 @@ from oracle import pyoracle as po
 
 pytestmark = pytest.mark.gpu
 tp = pytest.importorskip("test_particle_gb300")
+import test_particle_gb300.workloads as wl  # noqa: E402
+
 SC = mg.scenarios()
 CASES = (0, 3, 4, 5)
 DIFF_INTERVAL = 100  # tinterval_dcoeffs, src/tracking.c:17
@@ -204,3 +209,104 @@ def test_single_step_loop(case):
         assert np.array_equal(eep.reshape(nt, nb), run["espect_escape"])
     assert np.array_equal(remain, run["remain"])
     np.testing.assert_allclose(d, run["dsum"], rtol=1e-10, atol=1e-30)
+
+
+def spectrum_file(path, nbins, nt_out):
+    rows = open(path).read().splitlines()
+    assert len(rows) == nt_out
+    vals = np.array([[float(x) for x in r.split()] for r in rows])
+    assert vals.shape == (nt_out, nbins)
+    return vals
+
+
+def bin_widths(nbins):
+    """The bin widths collect_espectrum divides by (src/diagnostics.c:221-248)."""
+    L = tp.lib()
+    emin = C.c_double.in_dll(L, "emin").value
+    logemin = C.c_double.in_dll(L, "logemin").value
+    logde = C.c_double.in_dll(L, "logde").value
+    w = np.empty(nbins)
+    w[0] = emin
+    for i in range(1, nbins):
+        w[i] = 10 ** logemin * (10 ** (logde * i) - 10 ** (logde * (i - 1)))
+    return w
+
+
+def hybrid(n, dt, nb, nt, bc, method, pi, nst, p):
+    L = lib()
+    L.particle_tracking_hybrid.argtypes = [I, I, D, I, I, I, I, D, V, I, I, V, V, V, V]
+    L.particle_tracking_hybrid(0, n, dt, nb, nt, bc, 1, 1.0, None, method, 0, ptr(pi), ptr(nst),
+                               ptr(p), None)
+
+
+@pytest.mark.parametrize("case", (0, 5))
+def test_tracking_hybrid_fixed_step(case, tmp_path, monkeypatch):
+    """src/tracking.c:659-699 with tracking_method 0: the run, then
+    data/espectrum.dat (and data/espect_escape.dat with open boundaries) as
+    counts per unit energy, and data/diff_coeffs.dat."""
+    tr, key, m = setup(case)
+    p0 = tr[key + "ptl0"]
+    n, nb, nt = len(p0), m["nbins"], m["nt_out"]
+    run = tp.track(p0, m["dt"], nt, nb, precision=tp.PREC_FP64)
+    monkeypatch.chdir(tmp_path)
+    (tmp_path / "data").mkdir()
+    pi, p = p0.copy(), p0.copy()
+    nst = np.zeros(n, np.int32)
+    hybrid(n, m["dt"], nb, nt, m["bc"], 0, pi, nst, p)
+    assert tp.device_status() == 0
+    same_particles(p, run["ptl"])
+    assert np.array_equal(nst, run["nsteps"])
+    w = bin_widths(nb)
+    got = spectrum_file(tmp_path / "data" / "espectrum.dat", nb, nt)
+    np.testing.assert_allclose(got, run["espect"] / w, rtol=6e-5, atol=0)
+    assert (tmp_path / "data" / "diff_coeffs.dat").exists()
+    esc = tmp_path / "data" / "espect_escape.dat"
+    if m["bc"] == 1:
+        got = spectrum_file(esc, nb, nt)
+        np.testing.assert_allclose(got, run["espect_escape"] / w, rtol=6e-5, atol=0)
+        assert got.sum() > 0
+    else:
+        assert not esc.exists()
+
+
+def test_tracking_hybrid_adaptive(tmp_path, monkeypatch):
+    """tracking_method 1 runs the adaptive Bulirsch-Stoer stepper in the
+    wire-loop field (the reference leaves this branch empty,
+    src/tracking.c:681-684): the same particles, step counts and spectrum as a
+    direct call of the batched stepper with u-form derivatives."""
+    s = SC["loop"]
+    n, nb, nt, h0, tmax = 512, 50, 4, 1e-6, 0.004
+    d = po.Domain.from_buffer_copy(s["dom"])
+    d.tmax = tmax
+    tp.configure(system_type=tp.SYS_WLCS, charge_mass=s["charge_mass"], bc_flag=2, dom=d,
+                 wl=s["wl"], ibessel=0)
+    tp.set_spectrum(nb, 1e-3, 1e1)
+    y0 = wl.torus_particles(n, 1.0, 0.05, 0.3, 0.1, 0.9, 11)
+    gam = 1.0 / np.sqrt(1.0 - (y0[:, 3:] ** 2).sum(axis=1))
+    p0 = np.zeros(n, dtype=tp.PARTICLE_DTYPE)
+    for k, c in enumerate(("x", "y", "z")):
+        p0[c] = y0[:, k]
+        p0["u" + c] = gam * y0[:, 3 + k]
+    p0["qm"] = s["charge_mass"]
+    monkeypatch.chdir(tmp_path)
+    (tmp_path / "data").mkdir()
+    pi, p = p0.copy(), p0.copy()
+    nst = np.zeros(n, np.int32)
+    hybrid(n, h0, nb, nt, 2, 1, pi, nst, p)
+    assert tp.device_status() == 0
+    y = np.stack([p0["x"], p0["y"], p0["z"], p0["ux"], p0["uy"], p0["uz"]], 1).copy()
+    t = np.zeros(n)
+    steps, st = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    esp, dfr = np.zeros(nt * nb), np.zeros(8 * (nt + 1))
+    tp.check(tp.lib().tp_bs_run(C.c_int(n), tp._ptr(y), tp._ptr(t), C.c_double(tmax), C.c_int(nt),
+                                C.c_int(nb), C.c_double(h0), C.c_double(1e-10), C.c_double(1e-10),
+                                C.c_int(8), C.c_int(1), C.c_int(10000000), tp._ptr(steps),
+                                tp._ptr(st), tp._ptr(esp), tp._ptr(dfr), None), "bs_run")
+    assert (st == 0).all()
+    assert np.all(t == tmax) and np.all(p["t"] == tmax)
+    for k, c in enumerate(("x", "y", "z", "ux", "uy", "uz")):
+        assert np.array_equal(p[c], y[:, k]), c
+    assert np.array_equal(nst, steps) and (steps > 0).all()
+    got = spectrum_file(tmp_path / "data" / "espectrum.dat", nb, nt)
+    np.testing.assert_allclose(got, esp.reshape(nt, nb) / bin_widths(nb), rtol=6e-5, atol=0)
+    assert esp.reshape(nt, nb).sum(axis=1).tolist() == [n] * nt
