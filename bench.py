@@ -359,6 +359,51 @@ def config_bench(name, args):
                            "diffusion_rel_err_noise_floor": dc_rel(runs["ref_perturbed"], runs["ref"]),
                            "diffusion_order": ["drr", "dxx", "dyy", "dzz", "dpp", "duu", "daa", "dee"]}
         sess.close()
+    elif name == "open":
+        # open boundaries: a 128^3 gridded field in an open box that most
+        # particles leave within the run; one launch against segments with the
+        # departed particles compacted away (identical results)
+        n = args.nptl or 262144
+        steps = args.run_steps or 4000
+        cfg = wl.config_grid(nptl=n, steps=steps, n=128, dx=0.25)
+        L = cfg["hi"][0]
+        dom = tp.Domain()
+        dom.xmax = dom.ymax = dom.zmax = L
+        dom.xmax_ptl = dom.ymax_ptl = dom.zmax_ptl = L
+        dom.tmax = steps * cfg["dt"] + 0.5 * cfg["dt"]
+        grd = tp.Grids()
+        grd.nx = grd.ny = grd.nz = 128
+        grd.nt = 1
+        grd.dx = grd.dy = grd.dz = 0.25
+        tp.configure(system_type=tp.SYS_PIC, charge_mass=1.0, bc_flag=1, dom=dom, grd=grd, mt=0)
+        mb = wl.kolmogorov_modes(cfg["nmodes"], cfg["kmin"], 16.0, cfg["dB"], cfg["seed"])
+        mv = wl.kolmogorov_modes(cfg["nmodes"], cfg["kmin"], 16.0, cfg["v_rms"], cfg["seed"] + 1000)
+        tp.synth_pic_fields(mb, mv, 1.0)
+        tp.set_spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
+        p0 = wl.shell_particles(n, cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"])
+        rates, res = {}, {}
+        for label, seg in (("one_launch", 0), ("compacted", -1)):
+            tp.lib().tp_set_compaction(C.c_int(seg))
+            best = None
+            for _ in range(3):
+                r = tp.track(p0, cfg["dt"], 10, cfg["nbins"], precision=tp.PREC_MIXED)
+                if best is None or r["info"].kernel_ms < best["info"].kernel_ms:
+                    best = r
+            res[label] = best
+            rates[label] = {"particle_steps_per_s": n * steps / best["info"].kernel_ms * 1e3,
+                            "kernel_ms": best["info"].kernel_ms, "launches": best["info"].launches}
+        tp.lib().tp_set_compaction(C.c_int(-1))
+        a, b = res["one_launch"], res["compacted"]
+        left = float(a["espect_escape"].sum())
+        out.update(workload="open_box_pic_128^3_%dptl_%dsteps" % (n, steps), rates=rates,
+                   departed_fraction=left / n,
+                   pushes_done=int(a["nsteps"].sum() - n),
+                   identical=bool(all(np.array_equal(a["ptl"][c], b["ptl"][c]) for c in ("x", "y", "z", "ux", "uy", "uz"))
+                                  and np.array_equal(a["espect"], b["espect"])
+                                  and np.array_equal(a["espect_escape"], b["espect_escape"])
+                                  and np.array_equal(a["remain"], b["remain"])),
+                   speedup=rates["one_launch"]["kernel_ms"] / rates["compacted"]["kernel_ms"])
+        tp.release_device_fields()
     elif name == "bs":
         # one circular loop (radius 1, current 1, no wire), E = 0; particles on a
         # torus around the wire, |v| in [0.1, 0.9] c; the reference's equations
@@ -419,7 +464,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=1)
-    ap.add_argument("--config", choices=["abc", "modesum", "surrogate", "bs"], default=None,
+    ap.add_argument("--config", choices=["abc", "modesum", "surrogate", "bs", "open"], default=None,
                     help="secondary workload instead of the headline line")
     ap.add_argument("--nptl", type=int, default=0)
     ap.add_argument("--run-steps", type=int, default=0)

@@ -314,6 +314,17 @@ int tp_read_pic_fields_binary(const char *filepath, int ct);
  * tp_synth_pic_fields) to host arrays of nx*ny*nz {x,y,z} float records. */
 int tp_fetch_device_fields(float *host_e, float *host_b);
 
+/* Open boundaries (bc_flag 1): fixed-step runs go in segments of `steps`
+ * steps (rounded up to a multiple of the 100-step diffusion interval) and the
+ * particles that left the box are dropped from the launches that follow, their
+ * remaining diagnostic contributions (the last diffusion singles the reference
+ * keeps adding, src/tracking.c:334-368, and the departure counts) added in
+ * closed form.  0: one launch for the whole run; -1 (default): about eight
+ * segments.  FP64 trajectories are unchanged by it; the order of the FP64
+ * diffusion sums is not.  Runs with trajectory diagnostics or the learned
+ * field, and runs that start after step 1, use one launch. */
+void tp_set_compaction(int steps);
+
 /* One call, host buffers in and out (reuses a cached session). */
 int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,
                   const particles *ptl_init, particles *ptl, int *nsteps_ptl,

@@ -398,6 +398,7 @@ extern "C" void tp_set_abc(double A, double B, double C)
 
 extern "C" void tp_set_interp_corrected(int on) { g.interp_corrected = on ? 1 : 0; }
 extern "C" void tp_set_ellint_corrected(int on) { g.ellint_corrected = on ? 1 : 0; }
+extern "C" void tp_set_compaction(int steps) { g.compact_steps = steps < 0 ? -1 : steps; }
 
 extern "C" int tp_set_modes(int nmodes, const tp_mode* modes, double Bz0)
 {

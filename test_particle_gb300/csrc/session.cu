@@ -1,5 +1,6 @@
 // session.cu -- device-resident tracking sessions: particle state in HBM as
 // SoA, one persistent tracking launch per run, diagnostics reduced on the GPU.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -30,10 +31,132 @@ static void fill_int(int* p, int n, int v, cudaStream_t s)
     if (n > 0) fill_int_kernel<<<(n + 255) / 256, 256, 0, s>>>(p, n, v);
 }
 
+// ---------------------------------------------------------------- open-boundary segments
+// Between the segments of an open-boundary run the particles still inside the
+// box are compacted into an index list, in list order and independent of
+// timing: per-block counts, one block that scans them and sums the departed
+// particles' carried diffusion singles in block order, then the scatter.
+constexpr int kCmpBlock = 1024;
+// singles the reference keeps adding for a particle that no longer moves
+// (dxx, dyy, dzz, daa, dee; drr, dpp, duu are cleared every step,
+// src/tracking.c:334-336)
+__constant__ int kStaleComp[5] = {1, 2, 3, 6, 7};
+
+// exclusive scan over a block of kCmpBlock threads; total = the block's sum
+__device__ __forceinline__ int block_excl_scan(int v, int* sh, int& total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = sh[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        sh[lane] = w;
+    }
+    __syncthreads();
+    const int before = (warp > 0 ? sh[warp - 1] : 0) + x - v;
+    total = sh[31];
+    __syncthreads();
+    return before;
+}
+
+__global__ void __launch_bounds__(kCmpBlock) seg_count_kernel(const int* idx, int n, const int* esc,
+                                                              const double* sg, int* cnt, double* part)
+{
+    __shared__ int sh[32];
+    __shared__ double red[32][5];
+    const int k = blockIdx.x * kCmpBlock + threadIdx.x;
+    int keep = 0;
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (k < n) {
+        const int i = idx ? idx[k] : k;
+        if (esc[i] == 0) {
+            keep = 1;
+        } else {
+#pragma unroll
+            for (int c = 0; c < 5; c++) v[c] = sg[(size_t)i * kSegCarry + kStaleComp[c]];
+        }
+    }
+    int total;
+    block_excl_scan(keep, sh, total);
+    if (threadIdx.x == 0) cnt[blockIdx.x] = total;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 5; c++) {
+        double x = v[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[warp][c] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        double t = 0.0;
+        for (int w = 0; w < 32; w++) t += red[w][threadIdx.x];
+        part[(size_t)blockIdx.x * 5 + threadIdx.x] = t;
+    }
+}
+
+// One block: offsets of the kept particles per count block, the new count,
+// and the departed particles' contributions to the diffusion rows row_lo ..
+// row_hi (their singles, added at every later diffusion step) and to the
+// remaining counts (one departure per later diffusion step), into `extra`,
+// a slot of partial sums laid out like one tracking block's.
+__global__ void __launch_bounds__(kCmpBlock) seg_scan_kernel(const int* cnt, const double* part, int nblk,
+                                                             int n, int* off, int* n_next, double* extra,
+                                                             int* remain, int nsdc, int row_lo, int row_hi)
+{
+    __shared__ int sh[32];
+    int carry = 0;
+    for (int b0 = 0; b0 < nblk; b0 += kCmpBlock) {
+        const int b = b0 + threadIdx.x;
+        const int v = b < nblk ? cnt[b] : 0;
+        int total;
+        const int pre = block_excl_scan(v, sh, total);
+        if (b < nblk) off[b] = carry + pre;
+        carry += total;
+    }
+    if (threadIdx.x == 0) {
+        *n_next = carry;
+        const int departed = n - carry;
+        double S[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int b = 0; b < nblk; b++)
+            for (int c = 0; c < 5; c++) S[c] += part[(size_t)b * 5 + c];
+        for (int r = row_lo; r <= row_hi && r < nsdc; r++) {
+            for (int c = 0; c < 5; c++) extra[(size_t)r * 8 + kStaleComp[c]] += S[c];
+            if (r + 1 < nsdc) remain[r + 1] -= departed;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kCmpBlock) seg_scatter_kernel(const int* idx, int n, const int* esc,
+                                                                const int* off, int* idx_out)
+{
+    __shared__ int sh[32];
+    const int k = blockIdx.x * kCmpBlock + threadIdx.x;
+    int keep = 0, i = 0;
+    if (k < n) {
+        i = idx ? idx[k] : k;
+        keep = esc[i] == 0;
+    }
+    int total;
+    const int pos = block_excl_scan(keep, sh, total);
+    if (keep) idx_out[off[blockIdx.x] + pos] = i;
+}
+
 Session::~Session()
 {
     for (Scratch* sc : {&soa, &soa0, &aos, &nsteps, &spec, &rem, &dpart, &dsum, &traj, &trajacc,
-                        &trajpts})
+                        &trajpts, &cmp})
         sc->release();
     for (cudaEvent_t e : {ev0, ev1, evb, eve})
         if (e) cudaEventDestroy(e);
@@ -121,16 +244,39 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
     int grid = g.num_sms * bps;
     if (grid > ntiles) grid = ntiles;
     if (grid < 1) grid = 1;
+    // open boundaries: segments of seg steps with the departed particles dropped
+    int seg = g.compact_steps > 0 ? g.compact_steps : std::max(kDiffInterval, rs.estep / 8);
+    seg = (seg + kDiffInterval - 1) / kDiffInterval * kDiffInterval;
+    const bool segs = bc_flag == 1 && g.compact_steps != 0 && rs.traj_every == 0 && !is_surr &&
+                      rs.sstep == 1 && rs.estep > seg && n > 0;
+    const int nslot = grid + (segs ? 1 : 0);  // the last slot takes the departed particles' rows
     size_t nspec = (size_t)nt_out * nbins;
     unsigned* d_spec = (unsigned*)spec.get(sizeof(unsigned) * 2 * nspec);
     int* d_rem = (int*)rem.get(sizeof(int) * nsdc);
-    double* d_dpart = (double*)dpart.get(sizeof(double) * 8 * (size_t)nsdc * grid);
+    double* d_dpart = (double*)dpart.get(sizeof(double) * 8 * (size_t)nsdc * nslot);
     double* d_dsum = (double*)dsum.get(sizeof(double) * 8 * (size_t)nsdc);
     if (!d_spec || !d_rem || !d_dpart || !d_dsum) return false;
+    const size_t nblk_max = ((size_t)n + kCmpBlock - 1) / kCmpBlock;
+    double *c_sg = nullptr, *c_part = nullptr;
+    int *c_idx0 = nullptr, *c_idx1 = nullptr, *c_esc = nullptr, *c_cnt = nullptr, *c_off = nullptr,
+        *c_n = nullptr;
+    if (segs) {
+        char* c = (char*)cmp.get(sizeof(double) * ((size_t)kSegCarry * n + 5 * nblk_max) +
+                                 sizeof(int) * (3 * (size_t)n + 2 * nblk_max + 1));
+        if (!c) return false;
+        c_sg = (double*)c;
+        c_part = c_sg + (size_t)kSegCarry * n;
+        c_idx0 = (int*)(c_part + 5 * nblk_max);
+        c_idx1 = c_idx0 + n;
+        c_esc = c_idx1 + n;
+        c_cnt = c_esc + n;
+        c_off = c_cnt + nblk_max;
+        c_n = c_off + nblk_max;
+    }
     cudaEventRecord(evb, s);
     cudaMemsetAsync(d_spec, 0, sizeof(unsigned) * 2 * nspec, s);
     cudaMemsetAsync(d_rem, 0, sizeof(int) * nsdc, s);
-    cudaMemsetAsync(d_dpart, 0, sizeof(double) * 8 * (size_t)nsdc * grid, s);
+    cudaMemsetAsync(d_dpart, 0, sizeof(double) * 8 * (size_t)nsdc * nslot, s);
     if (rs.reset_nsteps) fill_int((int*)nsteps.ptr, n, 1, s);
 
     TrackBufs b;
@@ -157,6 +303,7 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
         b.ntraj_total = traj_total;
     }
     TrackParams q;
+    memset(&q, 0, sizeof(q));
     q.n = n;
     q.estep = rs.estep;
     q.einterval = rs.einterval;
@@ -168,14 +315,61 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
     q.sstep = rs.sstep;
     q.traj_every = rs.traj_every;
     q.dt = rs.dt;
+    auto launch = [&](const TrackParams& qq, int gr) {
+        return rs.precision == TP_PREC_FP64 ? fp64::launch_track(f, b, qq, gr, s)
+             : is_mixed ? mixed::launch_track(mf, b, qq, gr, s)
+             : is_surr  ? mlp::launch_track_surrogate(mf, md, b, qq, gr, s)
+                        : fp64fast::launch_track(f, b, qq, gr, s);
+    };
+    int launches = 1;
     cudaEventRecord(ev0, s);
-    cudaError_t e = rs.precision == TP_PREC_FP64 ? fp64::launch_track(f, b, q, grid, s)
-                  : is_mixed ? mixed::launch_track(mf, b, q, grid, s)
-                  : is_surr  ? mlp::launch_track_surrogate(mf, md, b, q, grid, s)
-                             : fp64fast::launch_track(f, b, q, grid, s);
-    if (!cuda_ok(e, "track launch")) return false;
+    if (!segs) {
+        if (!cuda_ok(launch(q, grid), "track launch")) return false;
+    } else {
+        b.sg_carry = c_sg;
+        b.esc_out = c_esc;
+        double* extra = d_dpart + (size_t)grid * nsdc * 8;
+        int n_act = n;
+        const int* cur = nullptr;
+        int* nxt = c_idx0;
+        launches = 0;
+        for (int s0 = rs.sstep;;) {
+            const int e0 = std::min(rs.estep, s0 + seg - 1);
+            TrackParams qs = q;
+            qs.sstep = s0;
+            qs.estep = e0;
+            qs.n = n_act;
+            qs.ntiles = (n_act + kBlock - 1) / kBlock;
+            qs.row0 = (s0 - 1) / kDiffInterval;
+            qs.resumed = s0 > rs.sstep;
+            qs.idx = cur;
+            // frame index: the reference's start value plus the frames already taken
+            if (qs.resumed) qs.ntp0 = q.ntp0 + (s0 - 1) / rs.einterval;
+            if (!cuda_ok(launch(qs, std::min(grid, qs.ntiles)), "track launch")) return false;
+            launches++;
+            if (e0 >= rs.estep) break;
+            const int nblk = (n_act + kCmpBlock - 1) / kCmpBlock;
+            seg_count_kernel<<<nblk, kCmpBlock, 0, s>>>(cur, n_act, c_esc, c_sg, c_cnt, c_part);
+            seg_scan_kernel<<<1, kCmpBlock, 0, s>>>(c_cnt, c_part, nblk, n_act, c_off, c_n, extra, d_rem,
+                                                    nsdc, e0 / kDiffInterval + 1, rs.estep / kDiffInterval);
+            seg_scatter_kernel<<<nblk, kCmpBlock, 0, s>>>(cur, n_act, c_esc, c_off, nxt);
+            int h_n = 0;
+            cudaMemcpyAsync(&h_n, c_n, sizeof(int), cudaMemcpyDeviceToHost, s);
+            if (!cuda_ok(cudaStreamSynchronize(s), "segment compaction")) return false;
+            launches += 3;
+            if (h_n < 0 || h_n > n_act) {
+                set_error(1, "segment compaction: %d of %d particles", h_n, n_act);
+                return false;
+            }
+            if (h_n == 0) break;  // every particle has left; its later rows are in `extra`
+            n_act = h_n;
+            cur = nxt;
+            nxt = nxt == c_idx0 ? c_idx1 : c_idx0;
+            s0 = e0 + 1;
+        }
+    }
     cudaEventRecord(ev1, s);
-    if (!cuda_ok(fp64::launch_reduce_dpart(d_dpart, grid, nsdc, d_dsum, s), "reduce")) return false;
+    if (!cuda_ok(fp64::launch_reduce_dpart(d_dpart, nslot, nsdc, d_dsum, s), "reduce")) return false;
     cudaEventRecord(eve, s);
     if (!cuda_ok(cudaStreamSynchronize(s), "track")) return false;
     float ms = 0.f, ms_step = 0.f;
@@ -192,7 +386,7 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
         info->blocks_per_sm = bps;
         info->kernel_ms = ms;
         info->step_ms = ms_step;
-        info->launches = rs.reset_nsteps ? 3 : 2;
+        info->launches = launches + (rs.reset_nsteps ? 2 : 1);
         info->pushes = (double)n * (rs.estep - rs.sstep + 1);
     }
     return true;

@@ -50,6 +50,12 @@ struct TrackBufs {
     unsigned int *espect_esc;     // nt_out * nbins counts (open boundary)
     int *remain;                  // nsdc
     double *dpart;                // gridDim.x * nsdc * 8 per-block partial sums (scratch)
+    // open-boundary runs in segments (null otherwise): per-particle state
+    // carried from one segment to the next (kSegCarry doubles: the diffusion
+    // singles, then what the mixed kernel needs to resume exactly), and the
+    // escape flag at the end of the segment
+    double *sg_carry;
+    int *esc_out;
     int *status;                  // error word
     // trajectory diagnostics (traj_every > 0): particles records written every
     // traj_every steps at ptl_time[offset(i) + point], offset(i) = ntraj_accum[i-1]
@@ -72,10 +78,17 @@ struct TrackParams {
     int sstep;       // first step index (the reference starts at 1)
     int traj_every;  // nsteps_output when trajectory diagnostics are on, else 0
     double dt;
+    // a segment of an open-boundary run (all zero for a whole run): diffusion
+    // rows used before it, whether it continues a run (no initial escape
+    // accounting), and the list of the q.n particles still inside the box
+    int row0;
+    int resumed;
+    const int* idx;
 };
 
 constexpr int kDiffInterval = 100;  // tinterval_dcoeffs, src/tracking.c:34
 constexpr int kBlock = 128;         // threads per block of the tracking kernels
+constexpr int kSegCarry = 16;      // doubles per particle carried between segments
 constexpr int kMaxSmemBins = 4096;  // per-frame block histogram in shared memory
 
 // status bits

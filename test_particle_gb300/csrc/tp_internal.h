@@ -38,6 +38,7 @@ struct Ctx {
     double ffA = 1.0, ffB = 0.81649658092772603, ffC = 0.57735026918962573;
     int interp_corrected = 0, ellint_corrected = 0;
     unsigned int wait_limit = 0;  // tensor-core pipeline hand-over polls (0: default)
+    int compact_steps = -1;       // open-boundary segment length (0: off, -1: automatic)
     std::vector<tp_mode> modes;
     double mode_B0 = 1.0;
     long modes_gen = 0;

@@ -25,6 +25,7 @@ struct Session {
     Scratch soa, soa0, aos, nsteps;
     Scratch spec, rem, dpart, dsum;
     Scratch traj, trajacc, trajpts;
+    Scratch cmp;             // open-boundary segments: index lists, flags, carried singles
     long traj_total = 0;
     int nt_out = 0, nbins = 0, nsdc = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evb = nullptr, eve = nullptr;

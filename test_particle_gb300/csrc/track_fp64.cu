@@ -227,8 +227,9 @@ __global__ void __launch_bounds__(kBlock) track_kernel(DevField f, TrackBufs b, 
     __shared__ unsigned int hist[kMaxSmemBins];
     const bool smem_hist = q.nbins <= kMaxSmemBins;
     for (int tile = blockIdx.x; tile < q.ntiles; tile += gridDim.x) {
-        const int i = tile * kBlock + threadIdx.x;
-        const bool active = i < q.n;
+        const int slot = tile * kBlock + threadIdx.x;
+        const bool active = slot < q.n;
+        const int i = active && q.idx ? q.idx[slot] : slot;  // the particle of this lane
         P64 p = {}, p0 = {};
         int nst = 1;
         if (active) {
@@ -240,9 +241,13 @@ __global__ void __launch_bounds__(kBlock) track_kernel(DevField f, TrackBufs b, 
         int esc_pre = 0;
         if (active) particle_bc(f, p, esc_pre);
         int esc_after = esc_pre;
-        int ntp = q.ntp0, tstep = 1;
+        int ntp = q.ntp0, tstep = 1 + q.row0;
         double sg[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-        if (active && esc_pre) atomicSub(&b.remain[1], 1);
+        if (active && q.resumed && b.sg_carry) {
+#pragma unroll
+            for (int c = 0; c < 8; c++) sg[c] = b.sg_carry[(size_t)i * kSegCarry + c];
+        }
+        if (active && esc_pre && !q.resumed) atomicSub(&b.remain[1], 1);
         double* slot_base = b.dpart + (size_t)blockIdx.x * q.nsdc * 8;
         int npts = 1;
         long toff = 0;
@@ -302,9 +307,16 @@ __global__ void __launch_bounds__(kBlock) track_kernel(DevField f, TrackBufs b, 
             esc_pre = esc_after;
         }
         if (active) {
-            store(b, i, p);
-            b.nsteps_ptl[i] = nst;
-            if (q.traj_every > 0) b.ntraj_points[i] = npts;
+            // the index again from the list rather than held through the loop
+            const int ie = q.idx ? q.idx[tile * kBlock + threadIdx.x] : tile * kBlock + threadIdx.x;
+            store(b, ie, p);
+            b.nsteps_ptl[ie] = nst;
+            if (q.traj_every > 0) b.ntraj_points[ie] = npts;
+            if (b.sg_carry) {
+#pragma unroll
+                for (int c = 0; c < 8; c++) b.sg_carry[(size_t)ie * kSegCarry + c] = sg[c];
+            }
+            if (b.esc_out) b.esc_out[ie] = esc_after;
         }
     }
 }

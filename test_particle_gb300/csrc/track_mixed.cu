@@ -58,8 +58,9 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
     const bool smem_hist = q.nbins <= kMaxSmemBins;
     const float dt = (float)q.dt;
     for (int tile = blockIdx.x; tile < q.ntiles; tile += gridDim.x) {
-        const int i = tile * kBlock + tx;
-        const bool active = i < q.n;
+        const int slot = tile * kBlock + tx;
+        const bool active = slot < q.n;
+        const int i = active && q.idx ? q.idx[slot] : slot;  // the particle of this lane
         PM p = {};
         FieldCache fc;
         int nst = 1;
@@ -93,13 +94,28 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
                 X0[k] = __double2ull_rz((r - floor(r)) * 18446744073709551616.0);
             }
             dg[DG_MU0][tx] = pitch_mu<SYS>(f, X0, uf0, smodes, fc);
+            if (q.resumed && b.sg_carry) {
+                // continue exactly where the previous segment stopped: the
+                // 64-bit fixed-point position and period counts, the start
+                // time and the steps taken (t = t0 + steps * dt)
+                const double* cr = b.sg_carry + (size_t)i * kSegCarry;
+#pragma unroll
+                for (int c = 0; c < 8; c++) dg[DG_SG + c][tx] = cr[c];
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    p.X[k] = (uint64_t)__double_as_longlong(cr[8 + k]);
+                    p.img[k] = (int)cr[11 + k];
+                }
+                dg[DG_T0][tx] = cr[14];
+            }
         }
         int esc_pre = esc ? 1 : 0;
         int esc_after = esc_pre;
-        int ntp = q.ntp0, tstep = 1;
-        if (active && esc_pre) atomicSub(&b.remain[1], 1);
+        int ntp = q.ntp0, tstep = 1 + q.row0;
+        if (active && esc_pre && !q.resumed) atomicSub(&b.remain[1], 1);
         double* slot_base = b.dpart + (size_t)blockIdx.x * q.nsdc * 8;
         int done = 0;
+        if (active && q.resumed && b.sg_carry) done = (int)b.sg_carry[(size_t)i * kSegCarry + 15];
         // countdowns to the next diagnostic steps (j % einterval, j % 100)
         int to_frame = q.einterval - q.sstep % q.einterval;
         int to_diff = kDiffInterval - q.sstep % kDiffInterval;
@@ -189,6 +205,19 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
             b.ux[i] = p.u[0]; b.uy[i] = p.u[1]; b.uz[i] = p.u[2];
             b.t[i] = dg[DG_T0][tx] + done * q.dt;
             b.nsteps_ptl[i] = nst;
+            if (b.sg_carry) {
+                double* cr = b.sg_carry + (size_t)i * kSegCarry;
+#pragma unroll
+                for (int c = 0; c < 8; c++) cr[c] = dg[DG_SG + c][tx];
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    cr[8 + k] = __longlong_as_double((long long)p.X[k]);
+                    cr[11 + k] = (double)p.img[k];
+                }
+                cr[14] = dg[DG_T0][tx];
+                cr[15] = (double)done;
+            }
+            if (b.esc_out) b.esc_out[i] = esc_after;
         }
     }
 }
