@@ -341,7 +341,9 @@ int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,
  * capture).  Calls that overlap on the GPU race on the shared scratch:
  * serialise them.  Runs the mixed-precision tracking kernel (TP_PREC_MIXED)
  * over steps 1..estep, system type 2 (ABC field from abc, B0, lambda0) or 4
- * (node-interleaved grid).  The return value is 0 on success, else one of
+ * (node-interleaved grid), in one launch also with open boundaries (it does
+ * not compact departed particles; the results equal the session's either
+ * way).  The return value is 0 on success, else one of
  * TP_NOALLOC_*; it does not wait for the kernels. */
 enum {
     TP_NOALLOC_EINVAL = 1,   /* bad argument (pointer, size, range)           */
