@@ -319,10 +319,12 @@ int tp_fetch_device_fields(float *host_e, float *host_b);
  * particles that left the box are dropped from the launches that follow, their
  * remaining diagnostic contributions (the last diffusion singles the reference
  * keeps adding, src/tracking.c:334-368, and the departure counts) added in
- * closed form.  0: one launch for the whole run; -1 (default): about eight
- * segments.  FP64 trajectories are unchanged by it; the order of the FP64
- * diffusion sums is not.  Runs with trajectory diagnostics or the learned
- * field, and runs that start after step 1, use one launch. */
+ * closed form.  0: one launch for the whole run; -1 (default): segments only
+ * when the particles' tiles take more than one wave of the launch, about 8
+ * for the mixed path and 32 for the FP64 paths.  Results are unchanged (the
+ * mixed path carries its fixed-point state across); only the order of the
+ * FP64 diffusion sums changes.  Runs with trajectory diagnostics or the
+ * learned field, and runs that start after step 1, use one launch. */
 void tp_set_compaction(int steps);
 
 /* One call, host buffers in and out (reuses a cached session). */

@@ -125,16 +125,20 @@ __global__ void __launch_bounds__(kCmpBlock) seg_scan_kernel(const int* cnt, con
         if (b < nblk) off[b] = carry + pre;
         carry += total;
     }
-    if (threadIdx.x == 0) {
-        *n_next = carry;
-        const int departed = n - carry;
-        double S[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        for (int b = 0; b < nblk; b++)
-            for (int c = 0; c < 5; c++) S[c] += part[(size_t)b * 5 + c];
-        for (int r = row_lo; r <= row_hi && r < nsdc; r++) {
-            for (int c = 0; c < 5; c++) extra[(size_t)r * 8 + kStaleComp[c]] += S[c];
-            if (r + 1 < nsdc) remain[r + 1] -= departed;
-        }
+    // one thread per component sums the blocks in order; one thread per row
+    __shared__ double S[5];
+    if (threadIdx.x < 5) {
+        double t = 0.0;
+        for (int b = 0; b < nblk; b++) t += part[(size_t)b * 5 + threadIdx.x];
+        S[threadIdx.x] = t;
+    }
+    if (threadIdx.x == 0) *n_next = carry;
+    __syncthreads();
+    const int departed = n - carry;
+    for (int r = row_lo + (int)threadIdx.x; r <= row_hi && r < nsdc; r += kCmpBlock) {
+#pragma unroll
+        for (int c = 0; c < 5; c++) extra[(size_t)r * 8 + kStaleComp[c]] += S[c];
+        if (r + 1 < nsdc) remain[r + 1] -= departed;
     }
 }
 
@@ -244,11 +248,17 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
     int grid = g.num_sms * bps;
     if (grid > ntiles) grid = ntiles;
     if (grid < 1) grid = 1;
-    // open boundaries: segments of seg steps with the departed particles dropped
-    int seg = g.compact_steps > 0 ? g.compact_steps : std::max(kDiffInterval, rs.estep / 8);
+    // open boundaries: segments of seg steps with the departed particles
+    // dropped.  Automatic mode: only when the tiles take more than one wave of
+    // the grid (within one wave an idle lane costs nothing), about 8 segments
+    // for the mixed path and 32 for the FP64 paths, whose steps cost ~60x more
+    // against the fixed cost of a segment (measured on an open 128^3 box).
+    const bool automatic = g.compact_steps < 0;
+    int seg = !automatic ? g.compact_steps
+                         : std::max(kDiffInterval, rs.estep / (is_mixed ? 8 : 32));
     seg = (seg + kDiffInterval - 1) / kDiffInterval * kDiffInterval;
     const bool segs = bc_flag == 1 && g.compact_steps != 0 && rs.traj_every == 0 && !is_surr &&
-                      rs.sstep == 1 && rs.estep > seg && n > 0;
+                      rs.sstep == 1 && rs.estep > seg && n > 0 && (!automatic || ntiles > grid);
     const int nslot = grid + (segs ? 1 : 0);  // the last slot takes the departed particles' rows
     size_t nspec = (size_t)nt_out * nbins;
     unsigned* d_spec = (unsigned*)spec.get(sizeof(unsigned) * 2 * nspec);
