@@ -605,7 +605,11 @@ def main():
                          "traffic": DRAM_BYTES_PER_PUSH * pushes,
                          "traffic_note": "ncu DRAM bytes of the 256^3 case scaled by pushes per launch",
                          "kernel": "track_mixed_kernel<PIC>",
-                         "algorithmic_bytes_per_push": 384},
+                         "algorithmic_bytes_per_push": 384,
+                         # the gathers above 1.0 are served by the register cell cache,
+                         # L1 and L2; what reaches DRAM is the traffic over the same time
+                         "dram_gbs": DRAM_BYTES_PER_PUSH * pushes / kernel_s / 1e9,
+                         "dram_frac": DRAM_BYTES_PER_PUSH * pushes / kernel_s / 1e9 / hbm},
             "fp64": {"value": fp64_value * world, "unit": UNIT,
                      "mixed_over_fp64": value / (fp64_value * world),
                      "spectrum_l1_mixed_vs_fp64": spec_l1,
