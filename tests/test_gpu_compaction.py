@@ -106,3 +106,31 @@ def test_open_box_segments(precision):
     assert 0.2 * len(p0) < left < len(p0)
     # departures counted at the diffusion steps up to step 500
     assert len(p0) - left <= one["remain"][-1] < len(p0)
+
+
+def test_every_particle_leaves():
+    """Uniform field along z, open unit box, every particle drifting out
+    through the z faces within about 400 of 800 steps: the segments stop once
+    the box is empty, and the later diffusion rows and remaining counts come
+    from the closed form alone."""
+    rng = np.random.default_rng(8)
+    n, dt, steps = 3000, 0.005, 800
+    dom = tp.Domain()
+    dom.xmax = dom.ymax = dom.zmax = 1.0
+    dom.xmax_ptl = dom.ymax_ptl = dom.zmax_ptl = 1.0
+    dom.tmax = steps * dt + 0.5 * dt
+    tp.configure(system_type=tp.SYS_TEST, charge_mass=1.0, bc_flag=1, dom=dom)
+    tp.set_spectrum(100, 1e-3, 1e1)
+    p0 = np.zeros(n, dtype=tp.PARTICLE_DTYPE)
+    p0["x"], p0["y"], p0["z"] = rng.uniform(0.3, 0.7, n), rng.uniform(0.3, 0.7, n), rng.uniform(0.0, 1.0, n)
+    uz = rng.uniform(0.6, 1.5, n) * np.where(rng.random(n) < 0.5, -1.0, 1.0)
+    p0["ux"], p0["uy"], p0["uz"] = 0.05 * rng.standard_normal(n), 0.05 * rng.standard_normal(n), uz
+    p0["qm"] = 1.0
+    for prec in (tp.PREC_FP64, tp.PREC_MIXED):
+        one = run(p0, dt, 4, 100, prec, 0)
+        cut = run(p0, dt, 4, 100, prec, 100)
+        same(cut, one)
+        assert one["espect_escape"].sum() == n  # everybody left
+        assert one["remain"][-1] == 0 and one["espect"][-1].sum() == 0
+        # 8 segments would take 8 + 7 x 3 + 2 = 31 launches; the box empties in the 4th
+        assert 3 < cut["info"].launches < 31
