@@ -383,7 +383,7 @@ def config_bench(name, args):
         p0 = wl.shell_particles(n, cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"])
         rates, res = {}, {}
         for label, seg in (("one_launch", 0), ("compacted", -1)):
-            tp.lib().tp_set_compaction(C.c_int(seg))
+            tp.set_compaction(seg)
             best = None
             for _ in range(3):
                 r = tp.track(p0, cfg["dt"], 10, cfg["nbins"], precision=tp.PREC_MIXED)
@@ -392,7 +392,7 @@ def config_bench(name, args):
             res[label] = best
             rates[label] = {"particle_steps_per_s": n * steps / best["info"].kernel_ms * 1e3,
                             "kernel_ms": best["info"].kernel_ms, "launches": best["info"].launches}
-        tp.lib().tp_set_compaction(C.c_int(-1))
+        tp.set_compaction(-1)
         a, b = res["one_launch"], res["compacted"]
         left = float(a["espect_escape"].sum())
         out.update(workload="open_box_pic_128^3_%dptl_%dsteps" % (n, steps), rates=rates,

@@ -218,6 +218,12 @@ def set_tmax(tmax):
     Domain.in_dll(lib(), "simul_domain").tmax = tmax
 
 
+def set_compaction(steps):
+    """Open-boundary runs in segments of `steps` steps with departed particles
+    dropped between them (0: one launch; -1: automatic)."""
+    lib().tp_set_compaction(C.c_int(int(steps)))
+
+
 def track(ptl_init, dt, nt_out, nbins, precision=PREC_FP64, ptl=None):
     """Fixed-step tracking of all particles on the GPU (host buffers in and out)."""
     L = lib()

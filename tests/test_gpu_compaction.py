@@ -3,7 +3,6 @@ compacted away (tp_set_compaction): the same particles, step counts,
 spectra and remaining counts as one launch over the whole run, diffusion sums
 equal to rounding (their summation order changes), in the FP64 parity path
 and in the mixed path."""
-import ctypes as C
 import json
 
 import numpy as np
@@ -23,11 +22,11 @@ COMPONENTS = ("x", "y", "z", "ux", "uy", "uz", "t", "xshift", "yshift", "zshift"
 @pytest.fixture(autouse=True)
 def _restore_default():
     yield
-    tp.lib().tp_set_compaction(C.c_int(-1))
+    tp.set_compaction(-1)
 
 
 def run(p0, dt, nt_out, nbins, precision, seg):
-    tp.lib().tp_set_compaction(C.c_int(seg))
+    tp.set_compaction(seg)
     r = tp.track(p0, dt, nt_out, nbins, precision=precision)
     assert tp.device_status() == 0
     return r
