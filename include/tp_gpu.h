@@ -205,6 +205,10 @@ void tp_mark_fields_dirty(void);
 
 /* Batch utilities, all on the GPU.  xyzt: n*4 doubles; particles: AoS records. */
 int tp_get_emf_batch(int n, const double *xyzt, double *emf6);
+/* The mixed-precision path's FP32 field (system types 0, 2, 4, 5) at n points
+ * (xyz: n*3 doubles, turned into 64-bit fixed point as the tracking kernel
+ * does), written as n*6 floats in emfields order (Bx, By, Bz, Ex, Ey, Ez). */
+int tp_get_emf_mixed_batch(int n, const double *xyz, float *emf6);
 int tp_wirz_steps(int n, particles *ptl, double dt, int nsteps, int *iescape);
 int tp_energy_bins(int n, const particles *ptl, int nbins, int *bins);
 int tp_calc_diff_coeff_batch(int n, const particles *ptl_init, const particles *ptl,
@@ -335,18 +339,22 @@ int tp_track_host(int precision, int nptl, double dt, int nt_out, int nbins,
 
 /* ---- Part 3: tracking without device allocation --------------------------
  * No counterpart in the reference.  For callers that may not allocate device
- * memory (a host framework whose allocator owns the GPU, a stream being
- * captured into a graph, a real-time host): the caller passes every input and
- * output as device memory; the library uses only a 4 MiB file-scope device
- * array for its scratch and calls no allocating routine.  The first call on
- * each device looks up that array's address (make it before any stream
- * capture).  Calls that overlap on the GPU race on the shared scratch:
- * serialise them.  Runs the mixed-precision tracking kernel (TP_PREC_MIXED)
- * over steps 1..estep, system type 2 (ABC field from abc, B0, lambda0) or 4
+ * memory (a host framework whose allocator owns every device allocation of
+ * the process, an embedded or real-time host that forbids allocation after
+ * start-up): the caller passes every input and output as device memory; the
+ * library uses only a 4 MiB file-scope device array for its scratch and calls
+ * no allocating routine.  The first call on each device looks up that
+ * array's address with the device current.  Calls on the same device share
+ * the scratch: calls that overlap on the GPU race on it, so serialise them,
+ * also across host threads; calls on different devices are independent.
+ * Runs the mixed-precision tracking kernel (TP_PREC_MIXED) over steps
+ * 1..estep, system type 2 (ABC field from abc, B0, lambda0) or 4
  * (node-interleaved grid), in one launch also with open boundaries (it does
  * not compact departed particles; the results equal the session's either
- * way).  The return value is 0 on success, else one of
- * TP_NOALLOC_*; it does not wait for the kernels. */
+ * way).  The return value is 0 on success, else one of TP_NOALLOC_*; it does
+ * not wait for the kernels.  Kernel-side conditions (device status bits as
+ * for tp_device_status, e.g. 2 for a non-finite momentum) are reported in
+ * *d_status when the caller passes one. */
 enum {
     TP_NOALLOC_EINVAL = 1,   /* bad argument (pointer, size, range)           */
     TP_NOALLOC_ETOOBIG = 2,  /* estep / 100 + 1 partial-sum rows do not fit   */
@@ -366,7 +374,7 @@ typedef struct tp_noalloc_args {
     double lo[3], hi[3];   /* box (xmin, ymin, zmin), (xmax, ymax, zmax)       */
     double abc[3], B0, lambda0;  /* ABC field (system 2)                       */
     const float *d_grid;   /* system 4: per node {Ex,Ey,Ez,0,Bx,By,Bz,0},
-                              x fastest, 16-byte aligned                       */
+                              x fastest, 32-byte aligned (one load per node)  */
     double *d_state;       /* in/out, 11 * n: the particles fields as columns
                               (x, y, z, qm, ux, uy, uz, t, xs, ys, zs)        */
     const double *d_state0;  /* 11 * n: the initial particles, same columns   */
@@ -377,6 +385,8 @@ typedef struct tp_noalloc_args {
                               dee) of estep / 100 + 1 diffusion sums          */
     int *d_remain;         /* out, estep / 100 + 1 particles remaining         */
     void *stream;          /* cudaStream_t, or NULL for the default stream    */
+    int *d_status;         /* optional out (device int): the kernel's status
+                              bits, cleared by the call; NULL: not reported   */
 } tp_noalloc_args;
 
 int tp_track_mixed_noalloc(const tp_noalloc_args *args);

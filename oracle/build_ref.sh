@@ -45,4 +45,6 @@ pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 # -Bsymbolic: the stepper's step() must not bind to glibc's legacy regexp step()
 "$CC" -shared -fopenmp -Wl,-Bsymbolic -o "$OUT/libtpref.so" "$OUT"/obj/*.o -lm
+# where the sources were: the fixture generator and the drop-in link test read it
+(cd "$REF" && pwd) > "$OUT/source_dir"
 echo "built $OUT/libtpref.so"

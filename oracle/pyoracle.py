@@ -91,9 +91,24 @@ def build_oracle(force=False):
 
 
 def build_ref():
-    """Compile the reference's own sources into oracle/_ref (needs the reference tree)."""
+    """Compile the reference's own sources into oracle/_ref (needs the reference
+    tree; the recipe says where it looks and exits without building when the
+    tree is absent)."""
     subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")])
     return LIB_REF if os.path.exists(LIB_REF) else None
+
+
+def reference_dir():
+    """The reference tree: $TP_REFERENCE_DIR, else the tree oracle/_ref was
+    last built from; None when neither names an existing tree."""
+    d = os.environ.get("TP_REFERENCE_DIR")
+    if not d:
+        try:
+            with open(os.path.join(HERE, "_ref", "source_dir")) as f:
+                d = f.read().strip()
+        except OSError:
+            d = None
+    return d if d and os.path.isdir(os.path.join(d, "src")) else None
 
 
 _oracle = None
@@ -190,6 +205,20 @@ def spectrum(nbins, emin, emax):
     s = OrSpectrum()
     oracle().or_spectrum_init(C.byref(s), C.c_int(nbins), C.c_double(emin), C.c_double(emax))
     return s
+
+
+def synth_pic_fields(modes_b, modes_v, B0z, nx, ny, nz, nthreads=0):
+    """The synthetic gridded (E, B) of the test workload on the CPU, as float
+    AoS arrays (n x 3 each), nodes x fastest."""
+    mb = np.ascontiguousarray(modes_b, dtype=MODE_DTYPE)
+    mv = np.ascontiguousarray(modes_v, dtype=MODE_DTYPE)
+    n = nx * ny * nz
+    e = np.zeros((n, 3), dtype=np.float32)
+    b = np.zeros((n, 3), dtype=np.float32)
+    oracle().or_synth_pic_fields(C.c_int(len(mb)), ptr(mb), C.c_int(len(mv)), ptr(mv),
+                                 C.c_double(B0z), C.c_int(nx), C.c_int(ny), C.c_int(nz), ptr(e), ptr(b),
+                                 C.c_int(nthreads))
+    return e, b
 
 
 def get_emf(f, xyzt):

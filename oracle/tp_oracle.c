@@ -407,6 +407,121 @@ void or_mode_sum(const or_field *f, double x, double y, double z, emfields *e)
     e->Ex = ef[0]; e->Ey = ef[1]; e->Ez = ef[2];
 }
 
+/* Synthetic gridded fields.  Node (i, j, k) of a grid periodic in node
+ * index has box coordinates u = (i/nx, j/ny, k/nz), held as exact 64-bit
+ * fixed point floor(i 2^64 / nx); a mode's phase is the exact integer
+ * n . U + phase0 (mod 2^64), phase0 = round(phase / 2 pi * 2^32) 2^32.  The
+ * cosine of that angle is formed as the real part of a product of four unit
+ * complex numbers, one per axis (exact per-axis angles) and one for phase0,
+ * so a row of nodes costs two multiplies and an add per mode instead of a
+ * cosine; the modes are summed per node in table order.  The product differs
+ * from the cosine of the summed angle by a few ulp, which moves a handful of
+ * the FP32 node values of a 512^3 grid by one FP32 ulp. */
+static void synth_axis(const tp_mode *m, int nm, int axis, int n, int idx, double *re, double *im)
+{
+    const uint64_t u = (uint64_t)(((unsigned __int128)idx << 64) / (unsigned)n);
+    for (int q = 0; q < nm; q++) {
+        uint64_t ph = (uint64_t)(int64_t)m[q].n[axis] * u;
+        double th = (double)(int64_t)ph * (2.0 * M_PI / 18446744073709551616.0);
+        re[q] = cos(th);
+        im[q] = sin(th);
+    }
+}
+
+static uint64_t synth_phase0(double phase)
+{
+    double rev = phase / (2.0 * M_PI);
+    rev -= floor(rev);
+    return (uint64_t)(uint32_t)llround(rev * 4294967296.0) << 32;
+}
+
+void or_synth_pic_fields(int nmb, const tp_mode *mb, int nmv, const tp_mode *mv, double B0z,
+                         int nx, int ny, int nz, float *e, float *b, int nthreads)
+{
+    const int nm = nmb + nmv;
+    tp_mode *all = (tp_mode *)malloc(sizeof(tp_mode) * (size_t)(nm > 0 ? nm : 1));
+    memcpy(all, mb, sizeof(tp_mode) * (size_t)nmb);
+    memcpy(all + nmb, mv, sizeof(tp_mode) * (size_t)nmv);
+    /* per mode: e^{i A_q(i)} along x for every i (SoA), and e^{i phase0} */
+    double *xr = (double *)malloc(sizeof(double) * (size_t)nm * nx);
+    double *xi = (double *)malloc(sizeof(double) * (size_t)nm * nx);
+    double *p0r = (double *)malloc(sizeof(double) * (size_t)(nm > 0 ? nm : 1));
+    double *p0i = (double *)malloc(sizeof(double) * (size_t)(nm > 0 ? nm : 1));
+    for (int q = 0; q < nm; q++) {
+        double th = (double)(int64_t)synth_phase0(all[q].phase) * (2.0 * M_PI / 18446744073709551616.0);
+        p0r[q] = cos(th);
+        p0i[q] = sin(th);
+    }
+    {
+        double *re = (double *)malloc(sizeof(double) * (size_t)(nm > 0 ? nm : 1));
+        double *im = (double *)malloc(sizeof(double) * (size_t)(nm > 0 ? nm : 1));
+        for (int i = 0; i < nx; i++) {
+            synth_axis(all, nm, 0, nx, i, re, im);
+            for (int q = 0; q < nm; q++) {
+                xr[(size_t)q * nx + i] = re[q];
+                xi[(size_t)q * nx + i] = im[q];
+            }
+        }
+        free(re);
+        free(im);
+    }
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+#endif
+    {
+        double *yr = (double *)malloc(sizeof(double) * (size_t)(nm > 0 ? nm : 1));
+        double *yi = (double *)malloc(sizeof(double) * (size_t)(nm > 0 ? nm : 1));
+        double *zr = (double *)malloc(sizeof(double) * (size_t)(nm > 0 ? nm : 1));
+        double *zi = (double *)malloc(sizeof(double) * (size_t)(nm > 0 ? nm : 1));
+        double *acc = (double *)malloc(sizeof(double) * 6 * (size_t)nx);
+        double *B0 = acc, *B1 = acc + nx, *B2 = acc + 2 * nx;
+        double *V0 = acc + 3 * nx, *V1 = acc + 4 * nx, *V2 = acc + 5 * nx;
+        int kz_last = -1;
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+        for (long row = 0; row < (long)ny * nz; row++) {
+            const int j = (int)(row % ny), k = (int)(row / ny);
+            if (k != kz_last) {
+                synth_axis(all, nm, 2, nz, k, zr, zi);
+                kz_last = k;
+            }
+            synth_axis(all, nm, 1, ny, j, yr, yi);
+            for (int c = 0; c < 6 * nx; c++) acc[c] = 0.0;
+            for (int q = 0; q < nm; q++) {
+                /* w = e^{iB} e^{iC} e^{i phase0} */
+                double ar = yr[q] * zr[q] - yi[q] * zi[q], ai = yr[q] * zi[q] + yi[q] * zr[q];
+                double wr = ar * p0r[q] - ai * p0i[q], wi = ar * p0i[q] + ai * p0r[q];
+                const double *qr = xr + (size_t)q * nx, *qi = xi + (size_t)q * nx;
+                const double a0 = all[q].amp_b[0], a1 = all[q].amp_b[1], a2 = all[q].amp_b[2];
+                double *o0 = q < nmb ? B0 : V0, *o1 = q < nmb ? B1 : V1, *o2 = q < nmb ? B2 : V2;
+#ifdef _OPENMP
+#pragma omp simd
+#endif
+                for (int i = 0; i < nx; i++) {
+                    const double c = wr * qr[i] - wi * qi[i];
+                    o0[i] += a0 * c;
+                    o1[i] += a1 * c;
+                    o2[i] += a2 * c;
+                }
+            }
+            float *eo = e + 3 * (size_t)row * nx, *bo = b + 3 * (size_t)row * nx;
+            for (int i = 0; i < nx; i++) {
+                const double Bx = B0[i], By = B1[i], Bz = B2[i] + B0z;
+                bo[3 * i] = (float)Bx;
+                bo[3 * i + 1] = (float)By;
+                bo[3 * i + 2] = (float)Bz;
+                eo[3 * i] = (float)(-(V1[i] * Bz - V2[i] * By));
+                eo[3 * i + 1] = (float)(-(V2[i] * Bx - V0[i] * Bz));
+                eo[3 * i + 2] = (float)(-(V0[i] * By - V1[i] * Bx));
+            }
+        }
+        free(yr); free(yi); free(zr); free(zi); free(acc);
+    }
+    free(xr); free(xi); free(p0r); free(p0i); free(all);
+}
+
 /* get_emf, src/emfields.c:32-60 (system 0: getemf_test :210-218; system 3:
  * getemf_mhd_test_particle :107-120; system 4: getemf_pic_test_particle :153-166) */
 void or_get_emf(const or_field *f, double x, double y, double z, double t, emfields *e)

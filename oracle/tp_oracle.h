@@ -61,6 +61,12 @@ int or_energy_bin_e(const or_spectrum *s, double ene);  /* bin of an energy gamm
 void or_calc_diff_coeff(const or_field *f, const particles *p0, const particles *p,
                         double dt, double out8[8]);
 void or_mode_sum(const or_field *f, double x, double y, double z, emfields *emf);
+/* The synthetic gridded E, B (no reference counterpart: the test workload's
+ * field) on the CPU, for the timed CPU baseline: B = B0z z + sum over mb,
+ * v = sum over mv, E = -v x B, at node (i, j, k) with phases
+ * 2 pi (n . (i/nx, j/ny, k/nz)) + phase, written as float AoS {x, y, z}. */
+void or_synth_pic_fields(int nmb, const tp_mode *mb, int nmv, const tp_mode *mv, double B0z,
+                         int nx, int ny, int nz, float *e, float *b, int nthreads);
 
 /* Batch helpers for ctypes callers. */
 void or_get_emf_batch(const or_field *f, int n, const double *xyzt, double *emf6);

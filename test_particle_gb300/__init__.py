@@ -175,6 +175,14 @@ def get_emf(xyzt):
     return out
 
 
+def get_emf_mixed(xyz):
+    """The mixed path's FP32 field at points (n x 3) -> n x 6 float32 (B, E)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros((len(xyz), 6), dtype=np.float32)
+    check(lib().tp_get_emf_mixed_batch(C.c_int(len(xyz)), _ptr(xyz), _ptr(out)), "get_emf_mixed")
+    return out
+
+
 def wirz_steps(ptl, dt, nsteps):
     p = np.array(ptl, dtype=PARTICLE_DTYPE, copy=True)
     esc = np.zeros(len(p), dtype=np.int32)
@@ -349,13 +357,15 @@ class Session:
               "session track")
         return info
 
-    def fetch(self, nt_out, nbins, nsdc):
-        p = np.zeros(self.n, dtype=PARTICLE_DTYPE)
+    def fetch(self, nt_out, nbins, nsdc, particles=True):
+        """Results of the last run; particles=False skips the particle state
+        and step counts (spectra, diffusion sums and remaining counts only)."""
+        p = np.zeros(self.n, dtype=PARTICLE_DTYPE) if particles else None
         esp = np.zeros(nt_out * nbins)
         ese = np.zeros(nt_out * nbins)
         dsum = np.zeros(8 * nsdc)
         rem = np.zeros(nsdc, dtype=np.int32)
-        nst = np.zeros(self.n, dtype=np.int32)
+        nst = np.zeros(self.n, dtype=np.int32) if particles else None
         check(self.L.tp_session_fetch(C.c_void_p(self.h), _ptr(p), _ptr(nst), _ptr(esp),
                                       _ptr(ese), _ptr(dsum), _ptr(rem)), "session fetch")
         return dict(ptl=p, espect=esp.reshape(nt_out, nbins), espect_escape=ese.reshape(nt_out, nbins),

@@ -164,3 +164,21 @@ bool build_mixfield(int stype, mixed::MixField& mf, int* nmodes_out)
 }
 
 }  // namespace tp
+
+using namespace tp;
+
+// The mixed path's FP32 field at n points (xyz: n*3 doubles) as n*6 floats
+// (Bx, By, Bz, Ex, Ey, Ez), for the current system type (0, 2, 4 or 5).
+extern "C" int tp_get_emf_mixed_batch(int n, const double* xyz, float* emf6)
+{
+    mixed::MixField mf;
+    if (!build_mixfield(system_type, mf, nullptr)) return -1;
+    if (n <= 0) return 0;
+    double* d_in = (double*)g.s_batch_a.get(sizeof(double) * 3 * (size_t)n);
+    float* d_out = (float*)g.s_batch_b.get(sizeof(float) * 6 * (size_t)n);
+    if (!d_in || !d_out) return -1;
+    cudaMemcpyAsync(d_in, xyz, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, g.stream);
+    if (!cuda_ok(mixed::launch_emf_batch(mf, n, d_in, d_out, g.stream), "emf mixed")) return -1;
+    cudaMemcpyAsync(emf6, d_out, sizeof(float) * 6 * (size_t)n, cudaMemcpyDeviceToHost, g.stream);
+    return cuda_ok(cudaStreamSynchronize(g.stream), "emf mixed sync") ? 0 : -1;
+}

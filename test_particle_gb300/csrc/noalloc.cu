@@ -3,23 +3,26 @@
 //
 // Some callers cannot call cudaMalloc: code that runs inside another
 // framework's memory pool or allocator (which owns every device allocation of
-// the process), code called while a stream is being captured into a CUDA
-// graph, where an allocation would break the capture, and embedded or
-// real-time hosts that forbid allocation after start-up.  They own their
-// particle and output buffers; this entry point adds nothing to them.  The
-// kernel's scratch -- the per-block partial sums of the diffusion
-// coefficients, the exact energy-bin edges and a status word -- lives in the
+// the process), and embedded or real-time hosts that forbid allocation after
+// start-up.  They own their particle and output buffers; this entry point
+// adds nothing to them.  The kernel's scratch -- the per-block partial sums
+// of the diffusion coefficients, the exact energy-bin edges and, when the
+// caller passes no status word of its own, a status word -- lives in the
 // file-scope device array below instead of in cudaMalloc'd memory.
 //
 // The array is kNoallocScratchBytes (4 MiB) on every GPU that loads the
 // library and stays allocated until the process exits.  Every call shares
 // it and it keeps the last call's contents; each call clears what must start
-// at zero.  Calls that overlap on the GPU (other streams, other host threads)
-// race on it: serialise them.
+// at zero.  Calls on the same device that overlap on the GPU (other streams,
+// other host threads) race on it: serialise them.  The bin edges travel to
+// the device as kernel arguments, so no host buffer outlives a call.
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
+#include <mutex>
 
 #include "../../include/tp_gpu.h"
 #include "tp_kernels.h"
@@ -38,10 +41,12 @@ constexpr int kMaxBins = 4096;
 static __device__ __align__(256) double tp_noalloc_scratch[kScratchDoubles];
 
 // Device address of the array for the current device, looked up once per
-// device with that device current (the first call on a device).
+// device with that device current (the first call on a device).  The lookup
+// table is shared by host threads, hence the lock (a std::mutex allocates
+// nothing).
 static double* g_scratch_addr[kMaxDevices];
 static bool g_scratch_ready[kMaxDevices];
-static double g_thr_host[kMaxBins];  // host staging of the bin edges (static, not heap)
+static std::mutex g_scratch_lock;
 
 static cudaError_t scratch_ptr(double** out)
 {
@@ -49,6 +54,7 @@ static cudaError_t scratch_ptr(double** out)
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_scratch_lock);
     if (!g_scratch_ready[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, tp_noalloc_scratch);
@@ -72,9 +78,24 @@ __global__ void add_kernel(int* p, int n, int v)
     if (i < n) p[i] += v;
 }
 
+// The bin edges reach the device by value, as the argument of a small
+// kernel, a chunk of kEdgeChunk edges per launch: the launch copies its
+// arguments, so the edges need neither a host staging buffer that must stay
+// valid until the copy runs nor a device allocation.
+constexpr int kEdgeChunk = 256;
+struct EdgeChunk {
+    double v[kEdgeChunk];
+};
+
+__global__ void put_edges_kernel(double* dst, EdgeChunk c, int n)
+{
+    int i = threadIdx.x;
+    if (i < n) dst[i] = c.v[i];
+}
+
 // The reference's bin of an energy (src/diagnostics.c:193-203, x86 semantics
 // for invalid conversions) and its exact edges by bisection on the bit
-// pattern, written into g_thr_host.
+// pattern, written into thr[0 .. nbins-2].
 static int ref_bin(double e, int nbins, double lmin, double lde)
 {
     double v = floor((log10(e) - lmin) / lde);
@@ -84,7 +105,7 @@ static int ref_bin(double e, int nbins, double lmin, double lde)
     return ib;
 }
 
-static bool edges(int nbins, double emin, double emax)
+static bool edges(int nbins, double emin, double emax, double* thr)
 {
     double lmin = log10(emin), lde = (log10(emax) - lmin) / (nbins - 2);
     if (!(lde > 0.0) || !std::isfinite(lmin)) return false;
@@ -103,7 +124,7 @@ static bool edges(int nbins, double emin, double emax)
             if (ref_bin(dm, nbins, lmin, lde) >= b) hi = mid;
             else lo = mid;
         }
-        memcpy(&g_thr_host[b - 1], &hi, sizeof(double));
+        memcpy(&thr[b - 1], &hi, sizeof(double));
     }
     return true;
 }
@@ -127,6 +148,14 @@ extern "C" int tp_track_mixed_noalloc(const tp_noalloc_args* a)
     if (a->system_type != TP_SYS_FORCEFREE && a->system_type != TP_SYS_PIC) return TP_NOALLOC_EINVAL;
     if (a->system_type == TP_SYS_PIC && (!a->d_grid || a->nx < 2 || a->ny < 2 || a->nz < 2 ||
                                          (unsigned long long)a->nx * a->ny * a->nz >= 0xffffffffull))
+        return TP_NOALLOC_EINVAL;
+    // alignment: a grid node is read with one 32-byte load, and every other
+    // buffer is read and written as its element type
+    auto misaligned = [](const void* p, uintptr_t al) { return ((uintptr_t)p & (al - 1)) != 0; };
+    if ((a->system_type == TP_SYS_PIC && misaligned(a->d_grid, 32)) || misaligned(a->d_state, 8) ||
+        misaligned(a->d_state0, 8) || misaligned(a->d_dsum, 8) || misaligned(a->d_nsteps, 4) ||
+        misaligned(a->d_espect, 4) || misaligned(a->d_espect_escape, 4) || misaligned(a->d_remain, 4) ||
+        misaligned(a->d_status, 4))
         return TP_NOALLOC_EINVAL;
     cudaStream_t s = static_cast<cudaStream_t>(a->stream);
 
@@ -173,7 +202,7 @@ extern "C" int tp_track_mixed_noalloc(const tp_noalloc_args* a)
     const int ntiles = (n + kBlock - 1) / kBlock;
     const int nsdc = a->estep / kDiffInterval + 1;
     const size_t thr_slots = ((size_t)(a->nbins - 1) + 31) / 32 * 32;
-    const size_t head = thr_slots + 32;  // edges, then a 256-byte slot for the status word
+    const size_t head = thr_slots + 32;  // edges, then a 256-byte slot for a status word
     int grid = nsm * bps;
     if (grid > ntiles) grid = ntiles;
     while (grid > 1 && head + (size_t)grid * nsdc * 8 > kScratchDoubles) grid--;
@@ -182,13 +211,22 @@ extern "C" int tp_track_mixed_noalloc(const tp_noalloc_args* a)
     double* scr = nullptr;
     if (scratch_ptr(&scr) != cudaSuccess) return TP_NOALLOC_ECUDA;
     double* d_thr = scr;
-    int* d_status = reinterpret_cast<int*>(scr + thr_slots);
+    // the kernel's status bits (TP_ST_*) go to the caller's word when it
+    // passes one, else to a slot of the scratch that nobody reads
+    int* d_status = a->d_status ? a->d_status : reinterpret_cast<int*>(scr + thr_slots);
     double* d_dpart = scr + head;
 
-    if (!edges(a->nbins, a->emin, a->emax)) return TP_NOALLOC_EINVAL;
+    double thr[kMaxBins];  // on the stack: edges for this call only
+    if (!edges(a->nbins, a->emin, a->emax, thr)) return TP_NOALLOC_EINVAL;
     const size_t nspec = (size_t)a->nt_out * a->nbins;
-    cudaError_t e = cudaMemcpyAsync(d_thr, g_thr_host, sizeof(double) * (a->nbins - 1),
-                                    cudaMemcpyHostToDevice, s);
+    cudaError_t e = cudaSuccess;
+    for (int c0 = 0; c0 < a->nbins - 1 && e == cudaSuccess; c0 += kEdgeChunk) {
+        EdgeChunk ch;
+        const int m = std::min(kEdgeChunk, a->nbins - 1 - c0);
+        memcpy(ch.v, thr + c0, sizeof(double) * m);
+        put_edges_kernel<<<1, kEdgeChunk, 0, s>>>(d_thr + c0, ch, m);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaMemsetAsync(d_status, 0, sizeof(int), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_dpart, 0, sizeof(double) * 8 * (size_t)nsdc * grid, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(a->d_espect, 0, sizeof(unsigned) * nspec, s);

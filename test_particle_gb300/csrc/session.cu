@@ -254,11 +254,14 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
     // for the mixed path and 32 for the FP64 paths, whose steps cost ~60x more
     // against the fixed cost of a segment (measured on an open 128^3 box).
     const bool automatic = g.compact_steps < 0;
-    int seg = !automatic ? g.compact_steps
-                         : std::max(kDiffInterval, rs.estep / (is_mixed ? 8 : 32));
-    seg = (seg + kDiffInterval - 1) / kDiffInterval * kDiffInterval;
+    // (64-bit: a segment length set near INT_MAX must not wrap when rounded up)
+    long long seg_ll = !automatic ? (long long)g.compact_steps
+                                  : (long long)std::max(kDiffInterval, rs.estep / (is_mixed ? 8 : 32));
+    seg_ll = (seg_ll + kDiffInterval - 1) / kDiffInterval * kDiffInterval;
     const bool segs = bc_flag == 1 && g.compact_steps != 0 && rs.traj_every == 0 && !is_surr &&
-                      rs.sstep == 1 && rs.estep > seg && n > 0 && (!automatic || ntiles > grid);
+                      rs.sstep == 1 && (long long)rs.estep > seg_ll && n > 0 &&
+                      (!automatic || ntiles > grid);
+    const int seg = (int)std::min<long long>(seg_ll, rs.estep);  // < estep whenever segs
     const int nslot = grid + (segs ? 1 : 0);  // the last slot takes the departed particles' rows
     size_t nspec = (size_t)nt_out * nbins;
     unsigned* d_spec = (unsigned*)spec.get(sizeof(unsigned) * 2 * nspec);
@@ -344,7 +347,7 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
         int* nxt = c_idx0;
         launches = 0;
         for (int s0 = rs.sstep;;) {
-            const int e0 = std::min(rs.estep, s0 + seg - 1);
+            const int e0 = (int)std::min<long long>(rs.estep, (long long)s0 + seg - 1);
             TrackParams qs = q;
             qs.sstep = s0;
             qs.estep = e0;

@@ -205,6 +205,8 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
             b.ux[i] = p.u[0]; b.uy[i] = p.u[1]; b.uz[i] = p.u[2];
             b.t[i] = dg[DG_T0][tx] + done * q.dt;
             b.nsteps_ptl[i] = nst;
+            if (b.status && !(isfinite(p.u[0]) && isfinite(p.u[1]) && isfinite(p.u[2])))
+                atomicOr(b.status, ST_NONFINITE);
             if (b.sg_carry) {
                 double* cr = b.sg_carry + (size_t)i * kSegCarry;
 #pragma unroll
@@ -220,6 +222,45 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
             if (b.esc_out) b.esc_out[i] = esc_after;
         }
     }
+}
+
+// The FP32 field of the mixed path at given points (tests and callers that
+// want the field the throughput path sees): each position is turned into
+// 64-bit fixed point exactly as the tracking kernel turns a particle's, and
+// the result is written as (Bx, By, Bz, Ex, Ey, Ez), the order of emfields.
+template <int SYS>
+__global__ void emf_mixed_batch_kernel(MixField f, int n, const double* __restrict__ xyz,
+                                       float* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint64_t X[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        double r = (xyz[3 * i + k] - f.min[k]) / f.L[k];
+        X[k] = __double2ull_rz((r - floor(r)) * 18446744073709551616.0);
+    }
+    FieldCache fc;
+    float E[3], B[3];
+    // the mode table is read from global memory here (the tracking kernel
+    // stages it in shared memory; the arithmetic is the same)
+    field_mixed<SYS>(f, X, E, B, f.modes, fc);
+    out[6 * i + 0] = B[0]; out[6 * i + 1] = B[1]; out[6 * i + 2] = B[2];
+    out[6 * i + 3] = E[0]; out[6 * i + 4] = E[1]; out[6 * i + 5] = E[2];
+}
+
+cudaError_t launch_emf_batch(const MixField& f, int n, const double* xyz, float* out, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const unsigned g = (unsigned)((n + 127) / 128);
+    switch (f.system_type) {
+    case TP_SYS_TEST: emf_mixed_batch_kernel<TP_SYS_TEST><<<g, 128, 0, s>>>(f, n, xyz, out); break;
+    case TP_SYS_FORCEFREE: emf_mixed_batch_kernel<TP_SYS_FORCEFREE><<<g, 128, 0, s>>>(f, n, xyz, out); break;
+    case TP_SYS_PIC: emf_mixed_batch_kernel<TP_SYS_PIC><<<g, 128, 0, s>>>(f, n, xyz, out); break;
+    case TP_SYS_MODESUM: emf_mixed_batch_kernel<TP_SYS_MODESUM><<<g, 128, 0, s>>>(f, n, xyz, out); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 // --------------------------------------------------------------- launchers

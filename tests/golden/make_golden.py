@@ -27,7 +27,6 @@ import numpy as np  # noqa: E402
 
 from oracle import pyoracle as po  # noqa: E402
 
-REF_DIR = os.environ.get("TP_REFERENCE_DIR", "/root/reference")
 PD = po.PARTICLE_DTYPE
 
 
@@ -242,9 +241,12 @@ def _bs_worker(args):
 
 
 def source_digest():
+    """Digest of the reference sources the fixtures came from (the tree that
+    oracle/build_ref.sh compiled, or $TP_REFERENCE_DIR)."""
+    ref_dir = po.reference_dir()
     h = hashlib.sha256()
     for sub in ("src", "src/unused", "include"):
-        dd = os.path.join(REF_DIR, sub)
+        dd = os.path.join(ref_dir, sub)
         for fn in sorted(os.listdir(dd)):
             fp = os.path.join(dd, fn)
             if os.path.isfile(fp):

@@ -8,11 +8,14 @@ import subprocess
 
 import pytest
 
+from oracle import pyoracle as po
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("TP_REFERENCE_DIR", "/root/reference")
+REF = po.reference_dir()
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")), reason="reference tree absent")
+@pytest.mark.skipif(REF is None, reason="reference tree absent: set TP_REFERENCE_DIR to it, or build "
+                                         "oracle/_ref from it first (oracle/build_ref.sh)")
 @pytest.mark.skipif(shutil.which("gcc") is None or shutil.which("objcopy") is None,
                     reason="gcc/objcopy absent")
 def test_reference_program_links_against_library(tmp_path):

@@ -133,3 +133,18 @@ def test_every_particle_leaves():
         assert one["remain"][-1] == 0 and one["espect"][-1].sum() == 0
         # 8 segments would take 8 + 7 x 3 + 2 = 31 launches; the box empties in the 4th
         assert 3 < cut["info"].launches < 31
+
+
+@pytest.mark.parametrize("seg", [2 ** 31 - 1, 2 ** 31 - 100])
+def test_segment_length_near_int_max_runs_one_launch(seg):
+    """A segment length near INT_MAX must not wrap when it is rounded up to
+    the 100-step diffusion interval: the run takes one tracking launch, the
+    same launches as with compaction off."""
+    cfg, p0 = _open_pic(n=1024, steps=300)
+    try:
+        one = run(p0, cfg["dt"], 3, 200, tp.PREC_MIXED, 0)
+        big = run(p0, cfg["dt"], 3, 200, tp.PREC_MIXED, seg)
+    finally:
+        tp.release_device_fields()
+    assert big["info"].launches == one["info"].launches
+    same(big, one)

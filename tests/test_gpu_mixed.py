@@ -66,21 +66,53 @@ def test_mixed_short_horizon_per_particle(kind, steps, tol):
     assert tp.device_status() == 0
 
 
+def _l1_frames(a, b, n):
+    """L1 distance of two spectra per output frame, each normalised by n."""
+    return np.abs(a / n - b / n).sum(axis=1)
+
+
+def sigma_l1(n):
+    """Standard deviation of the L1 distance of two independent n-particle
+    histograms (normal approximation of Poisson bin counts: each bin adds
+    |X - Y| with variance 2 lambda (1 - 2/pi), and the lambdas sum to n)."""
+    return np.sqrt(2.0 * (1.0 - 2.0 / np.pi) / n)
+
+
+def fp32_rounded(p0):
+    p = p0.copy()
+    for c in ("x", "y", "z", "ux", "uy", "uz"):
+        p[c] = p[c].astype(np.float32).astype(np.float64)
+    return p
+
+
 @pytest.mark.parametrize("kind", ["abc", "grid", "modesum"])
 def test_mixed_long_horizon_statistics(kind):
+    """Ensemble statistics over 2000 steps, 8192 particles.  The floor is the
+    FP64 path started from the initial state rounded to FP32 (the mixed path
+    keeps momenta in FP32): by chaos that FP64 run drifts away from the FP64
+    run as fast as the mixed run does.  Per output frame the mixed path's
+    spectrum L1 distance to FP64 must stay within 1.5x the floor's plus 3
+    sigma of the L1 statistic; per diffusion coefficient its largest row error
+    within max(1 %, 2x the floor's largest row error)."""
     cfg, p0 = setup(kind, 2000)
     a = tp.track(p0, cfg["dt"], 4, 200, precision=tp.PREC_FP64)
+    r = tp.track(fp32_rounded(p0), cfg["dt"], 4, 200, precision=tp.PREC_FP64)
     b = tp.track(p0, cfg["dt"], 4, 200, precision=tp.PREC_MIXED)
     n = len(p0)
-    sa, sb = a["espect"] / n, b["espect"] / n
-    assert abs(sa.sum() - sb.sum()) < 1e-12
-    l1 = np.abs(sa - sb).sum(axis=1)
-    # statistical noise floor of two decorrelated ensembles of n particles
-    assert np.all(l1 < 0.15), l1
-    scale = np.abs(a["dsum"][:, 1:]).max(axis=1, keepdims=True)
-    live = scale[:, 0] > 1e-12  # rows that are not rounding noise (dee with E = 0)
-    rel = np.abs(b["dsum"][live, 1:] - a["dsum"][live, 1:]) / scale[live]
-    assert np.median(rel) < 0.1
+    assert b["espect"].sum() == a["espect"].sum() == 4 * n
+    l1_mixed = _l1_frames(b["espect"], a["espect"], n)
+    l1_floor = _l1_frames(r["espect"], a["espect"], n)
+    print("%s L1 mixed %s floor %s 3sigma %.4f" % (kind, l1_mixed, l1_floor, 3 * sigma_l1(n)))
+    assert np.all(l1_mixed <= 1.5 * l1_floor + 3 * sigma_l1(n)), (l1_mixed, l1_floor)
+    ref = a["dsum"][:, 1:]
+    scale = np.abs(ref).max(axis=1)
+    live = scale > 1e-12 * np.abs(ref).max()  # dee with E = 0 is rounding noise in every path
+    for c in np.nonzero(live)[0]:
+        den = np.maximum(np.abs(ref[c]), 1e-300)
+        em = np.max(np.abs(b["dsum"][c, 1:] - ref[c]) / den)
+        ef = np.max(np.abs(r["dsum"][c, 1:] - ref[c]) / den)
+        print("%s diffusion row %d: mixed %.3e floor %.3e" % (kind, c, em, ef))
+        assert em <= max(0.01, 2.0 * ef), (c, em, ef)
     assert tp.device_status() == 0
 
 

@@ -107,13 +107,36 @@ def test_calc_diff_coeff():
     np.testing.assert_allclose(out, dc["out"], rtol=1e-11, atol=1e-14)
 
 
+def state_err(a, b):
+    """Largest per-particle difference of the unwrapped positions and the
+    momenta, relative to max(|value|, the largest |value| of that component
+    across particles x 1e-3)."""
+    worst = 0.0
+    for k in ("x", "y", "z"):
+        pa, pb = a[k] + a[k + "shift"], b[k] + b[k + "shift"]
+        den = np.maximum(np.abs(pb), 1e-3 * np.abs(pb).max() + 1e-300)
+        worst = max(worst, float(np.max(np.abs(pa - pb) / den)))
+    for k in ("ux", "uy", "uz"):
+        den = np.maximum(np.abs(b[k]), 1e-3 * np.abs(b[k]).max() + 1e-300)
+        worst = max(worst, float(np.max(np.abs(a[k] - b[k]) / den)))
+    return worst
+
+
+# per-particle state bounds of test_track_fixed, per golden case: uniform field
+# (0), ABC with and without a velocity grid (1, 2, 5), gridded PIC and MHD
+# fields (3, 4), wire-loop field (6)
+STATE_BOUND = {0: 1e-12, 1: 1e-6, 2: 1e-6, 3: 1e-6, 4: 1e-6, 5: 1e-6, 6: 1e-6}
+
+
 @pytest.mark.parametrize("case", range(7))
 def test_track_fixed(case):
-    """Whole fixed-step runs against the reference.  Gridded and uniform
-    fields: bit-exact.  Fields with sin/cos (ABC, wire loop): orbits are
-    chaotic, so ulp-level libm differences grow by ~e per 50 steps; parity is
-    checked on the early diffusion rows (within 500 steps) and on ensemble
-    statistics of the whole run."""
+    """Whole fixed-step runs against the reference's.  Step counts, remaining
+    counts and times are exact; every particle's final state is within the
+    case's bound; the pusher's sin/cos (and, for ABC and the wire loop, the
+    field's) differ from glibc in the last ulp, and orbits amplify that by
+    about e per 50 steps in the chaotic fields, so spectra are compared in
+    counts and the diffusion rows tightly early (within 500 steps) and loosely
+    over the whole run."""
     tr = load("track")
     key = "case%d_" % case
     m = json.loads(str(tr[key + "meta"]))
@@ -127,6 +150,12 @@ def test_track_fixed(case):
     assert np.array_equal(out["nsteps"], tr[key + "nsteps"])
     assert np.array_equal(out["remain"], tr[key + "remain"])
     assert np.array_equal(out["ptl"]["t"], ref_p["t"])
+    # per particle: the pusher calls sin/cos (and the analytic fields do), whose
+    # last-ulp differences from glibc grow with the orbit's sensitivity; the
+    # bound for each case is the measured growth with a 10x margin
+    err = state_err(out["ptl"], ref_p)
+    print("case %d (%s): per-particle max error %.3e" % (case, m["name"], err))
+    assert err <= STATE_BOUND[case], (case, err)
     # the pusher itself calls sin/cos, so no run is bit-exact over many steps
     assert out["espect"].sum() == tr[key + "espect"].sum()
     assert np.abs(out["espect"] - tr[key + "espect"]).sum() <= 2 * m["nt_out"]
@@ -152,7 +181,8 @@ def test_track_larger_vs_oracle():
     out = tp.track(p0, dt, 3, 200)
     f = mg.field_from(dict(s, dom=d))
     ref = po.track_fixed(f, po.spectrum(200, 1e-3, 1e2), p0, dt, 3, nthreads=0)
-    for k in ("x", "y", "z", "ux", "uy", "uz"):
-        assert np.median(np.abs(out["ptl"][k] - ref["ptl"][k])) < 1e-10
+    err = state_err(out["ptl"], ref["ptl"])
+    print("4096 particles x 300 steps, ABC: per-particle max error %.3e" % err)
+    assert err < 1e-6, err
     assert np.abs(out["espect"] - ref["espect"]).sum() <= 12
     np.testing.assert_allclose(out["dsum"], ref["dsum"], rtol=1e-6, atol=1e-20)

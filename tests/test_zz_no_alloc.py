@@ -1,8 +1,10 @@
 """tp_track_mixed_noalloc, the tracking entry point that allocates no device
-memory, against the session entry point of the same mixed-precision kernel
-(tp_track_host).  The caller owns every buffer (torch tensors here); two calls
-in a row must each reproduce the session's result, which also shows that
-each call clears the shared scratch it reuses."""
+memory, for callers whose host framework owns every device allocation or
+that may not allocate after start-up.  It is checked against the session
+entry point of the same mixed-precision kernel (tp_track_host).  The caller
+owns every buffer (torch tensors here), including the status word the kernel
+reports into; two calls in a row must each reproduce the session's result,
+which also shows that each call clears the shared scratch it reuses."""
 import ctypes as C
 
 import numpy as np
@@ -28,7 +30,7 @@ class NoallocArgs(C.Structure):
                 ("lambda0", C.c_double), ("d_grid", C.c_void_p), ("d_state", C.c_void_p),
                 ("d_state0", C.c_void_p), ("d_nsteps", C.c_void_p), ("d_espect", C.c_void_p),
                 ("d_espect_escape", C.c_void_p), ("d_dsum", C.c_void_p),
-                ("d_remain", C.c_void_p), ("stream", C.c_void_p)]
+                ("d_remain", C.c_void_p), ("stream", C.c_void_p), ("d_status", C.c_void_p)]
 
 
 def _fn():
@@ -82,7 +84,9 @@ def _case(kind, steps=300, n=4096, seed=21):
     return cfg, a, p0, grid
 
 
-def _run_noalloc(a, p0):
+def _run_noalloc(a, p0, status=None):
+    """One call on caller-owned buffers; `status` (a device int32 tensor, or
+    None for no status word) receives the kernel's status bits."""
     n = len(p0)
     nsdc = a.estep // 100 + 1
     cols = np.stack([np.ascontiguousarray(p0[c]) for c in COLS])
@@ -98,6 +102,7 @@ def _run_noalloc(a, p0):
     a.d_nsteps, a.d_espect, a.d_espect_escape = nsteps.data_ptr(), esp.data_ptr(), ese.data_ptr()
     a.d_dsum, a.d_remain = dsum.data_ptr(), rem.data_ptr()
     a.stream = torch.cuda.current_stream().cuda_stream
+    a.d_status = status.data_ptr() if status is not None else None
     torch.cuda.synchronize()
     free_before = torch.cuda.mem_get_info()[0]
     rc = _fn()(C.byref(a))
@@ -126,8 +131,11 @@ def test_noalloc_matches_session_twice(kind):
     cfg, a, p0, grid = _case(kind)
     ref = tp.track(p0, cfg["dt"], a.nt_out, a.nbins, precision=tp.PREC_MIXED)
     assert ref["estep"] == a.estep
-    first = _run_noalloc(a, p0)
-    second = _run_noalloc(a, p0)
+    assert tp.device_status() == 0  # the session run raised no status bit
+    st = torch.full((1,), -1, dtype=torch.int32, device="cuda")  # the call clears it
+    first = _run_noalloc(a, p0, status=st)
+    assert int(st.item()) == 0
+    second = _run_noalloc(a, p0)  # no status word: the call still runs
     # the first call on a device may load the library's kernels; later calls
     # leave the device's free memory as they found it
     assert second["free_change"] == 0
@@ -135,8 +143,25 @@ def test_noalloc_matches_session_twice(kind):
     _compare(second, ref)
     if kind == "pic":
         assert ref["espect_escape"].sum() > 0  # open boundary: some particles left
-    assert tp.device_status() == 0
     del grid
+
+
+def test_noalloc_reports_a_nonfinite_particle():
+    """A particle with a NaN momentum (every index the kernel forms from a
+    position stays inside the field whatever the value, so the run is safe)
+    raises status bit 2 in the caller's word; the other particles are
+    tracked as without it."""
+    cfg, a, p0, _ = _case("abc", steps=100, n=512)
+    bad = p0.copy()
+    bad["ux"][17] = np.nan
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    r = _run_noalloc(a, bad, status=st)
+    assert int(st.item()) & 2
+    clean = _run_noalloc(a, p0, status=st)
+    assert int(st.item()) == 0
+    keep = np.arange(len(p0)) != 17
+    for k in (4, 5, 6):  # ux, uy, uz of every other particle
+        assert np.array_equal(r["state"][k][keep], clean["state"][k][keep])
 
 
 def test_noalloc_rejects_bad_sizes():
@@ -155,5 +180,11 @@ def test_noalloc_rejects_bad_sizes():
     a.estep, a.nbins = 100, 5000
     assert _fn()(C.byref(a)) == EINVAL
     a.nbins, a.system_type = 200, tp.SYS_PIC  # no grid
+    assert _fn()(C.byref(a)) == EINVAL
+    a.nx = a.ny = a.nz = 2
+    a.d_grid = p + 16  # a node is one 32-byte load: the grid must be 32-byte aligned
+    assert _fn()(C.byref(a)) == EINVAL
+    a.d_grid = p
+    a.d_status = p + 2  # a status word must be 4-byte aligned
     assert _fn()(C.byref(a)) == EINVAL
     torch.cuda.synchronize()
