@@ -42,8 +42,8 @@ UNIT = "pushes/s"
 # particles x 200 steps): DRAM bytes read + written per push, and thread-level
 # instructions per push (smsp__inst_executed x 32 / pushes).  Summary:
 # profiles/track_mixed_kernel_pic_512cube_1048576ptl.txt
-DRAM_BYTES_PER_PUSH = (2.119311e9 + 10.339840e6) / 26214400.0
-INSTR_PER_PUSH = 491.0
+DRAM_BYTES_PER_PUSH = (20.12e9 + 89.65e6) / 209715200.0
+INSTR_PER_PUSH = 3055504469 * 32.0 / 209715200.0
 SMS, SCHEDULERS_PER_SM = 152, 4
 COEFFS = ["drr", "dxx", "dyy", "dzz", "dpp", "duu", "daa", "dee"]
 
@@ -163,14 +163,26 @@ def diffusion_errors(d_fast, d_ref):
     out."""
     ref = d_ref[:, 1:]
     fast = d_fast[:, 1:]
-    scale = np.abs(ref).max()
+    scale = np.nanmax(np.abs(ref))
     out = {}
     for c, name in enumerate(COEFFS):
-        if np.abs(ref[c]).max() <= 1e-12 * scale:
+        if np.nanmax(np.abs(ref[c])) <= 1e-12 * scale:
             continue
         rel = np.abs(fast[c] - ref[c]) / np.maximum(np.abs(ref[c]), 1e-300)
-        out[name] = {"max_over_rows": float(rel.max()), "final_row": float(rel[-1])}
+        bad = ~np.isfinite(rel)
+        # non-finite rows (a NaN sum) are counted, never printed as NaN
+        out[name] = {"max_over_rows": float(np.max(rel[~bad])) if (~bad).any() else None,
+                     "final_row": float(rel[-1]) if not bad[-1] else None,
+                     "nonfinite_rows": int(bad.sum())}
     return out
+
+
+def worst(dif):
+    """The largest relative error over coefficients and rows, inf if any row
+    was not finite."""
+    if any(v["nonfinite_rows"] for v in dif.values()):
+        return float("inf")
+    return max(v["max_over_rows"] for v in dif.values())
 
 
 def fp32_rounded(p0):
@@ -320,11 +332,11 @@ def gate_run(tp, wl, cfg, nptl, steps, seed):
     l1 = l1_frames(res["mixed"]["espect"], res["fp64"]["espect"])
     floor = sampling_floor(res["fp64"]["espect"])
     dif = diffusion_errors(res["mixed"]["dsum"], res["fp64"]["dsum"])
-    dmax = max(v["max_over_rows"] for v in dif.values())
+    dmax = worst(dif)
     out.update(particles=nptl, steps=steps, frame_steps=[100 * (k + 1) for k in range(nt_out)],
                spectrum_l1_mixed_vs_fp64_per_frame=l1, spectrum_l1_sampling_floor_per_frame=floor,
                l1_sigma=sigma_l1(nptl), diffusion_rel_err_mixed_vs_fp64=dif,
-               spectrum_l1_max=max(l1), diffusion_rel_err_max=dmax,
+               spectrum_l1_max=max(l1), diffusion_rel_err_max=dmax if np.isfinite(dmax) else None,
                met=bool(max(l1) <= 1e-3 and dmax <= 0.01),
                target="spectrum L1 <= 1e-3 at every frame and diffusion relative error <= 1 % at every "
                       "row, mixed path against the FP64 path on the same particles")

@@ -373,7 +373,7 @@ typedef struct tp_noalloc_args {
     double dt, charge_mass, emin, emax;
     double lo[3], hi[3];   /* box (xmin, ymin, zmin), (xmax, ymax, zmax)       */
     double abc[3], B0, lambda0;  /* ABC field (system 2)                       */
-    const float *d_grid;   /* system 4: per node {Ex,Ey,Ez,0,Bx,By,Bz,0},
+    const float *d_grid;   /* system 4: per node {Ex,Ey,Ez,Bx,By,Bz,0,0},
                               x fastest, 32-byte aligned (one load per node)  */
     double *d_state;       /* in/out, 11 * n: the particles fields as columns
                               (x, y, z, qm, ux, uy, uz, t, xs, ys, zs)        */

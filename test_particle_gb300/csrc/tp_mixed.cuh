@@ -27,10 +27,11 @@ struct MixField {
     uint32_t abc_m[3];       // lambda * L_k / 2pi
     uint32_t abc_off[3];     // lambda * min_k / 2pi in revolutions * 2^32
     float lam, lmin[3], lL[3];
-    // gridded fields: node-interleaved {E,0},{B,0} (PIC) or {v,0} (ABC velocity)
+    // gridded fields: node-interleaved {Ex,Ey,Ez,Bx,By,Bz,0,0} (PIC, 32 bytes a
+    // node) or {v,0} (ABC velocity)
     int nx, ny, nz;
     int interp_ref;          // 1: the reference's weights (x and z fractions exchanged)
-    const float4* eb;
+    const float4* eb;        // two float4 per node
     const float4* vgrid;
     // plane-wave mode sum, B = mB0 z + sum
     int nmodes;
@@ -76,11 +77,14 @@ __device__ __forceinline__ uint64_t fma_f2(uint64_t a, uint64_t b, uint64_t c)
     return r;
 }
 
-// 32 bytes from global memory through the read-only path in one load
-__device__ __forceinline__ void ld_node32(const float4* p, float4& a, float4& b)
+// One node {Ex,Ey,Ez,Bx,By,Bz,0,0} (32 bytes, 32-byte aligned) from global
+// memory through the read-only path in one 256-bit load, as three packed FP32
+// pairs (Ex,Ey) (Ez,Bx) (By,Bz); the padding pair is loaded and dropped.
+__device__ __forceinline__ void ld_node32(const float4* p, uint64_t& exy, uint64_t& ezbx, uint64_t& bybz)
 {
-    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+    uint64_t pad;
+    asm volatile("ld.global.nc.v4.b64 {%0,%1,%2,%3}, [%4];"
+                 : "=l"(exy), "=l"(ezbx), "=l"(bybz), "=l"(pad)
                  : "l"(p));
 }
 
@@ -92,6 +96,65 @@ struct CellCache {
     uint32_t key = 0xffffffffu;  // node index of the cached cell (grids hold < 2^32 - 1 nodes)
     float4 c[8 * STRIDE];
 };
+
+// The same for the gridded E and B: per corner the six components as three
+// packed FP32 pairs, 48 registers.
+struct CellCacheEB {
+    uint32_t key = 0xffffffffu;
+    uint64_t c[8][3];
+};
+
+// The cell of a position along one axis, with the reference's exchange of the
+// x and z fractions (src/interpolation.c:173-180) when interp_ref is set.
+__device__ __forceinline__ uint32_t cell_and_weights(const MixField& f, const uint64_t X[3], float w[8])
+{
+    int ix, iy, iz;
+    float fx, fy, fz;
+    cell_of(X[0], f.nx, ix, fx);
+    cell_of(X[1], f.ny, iy, fy);
+    cell_of(X[2], f.nz, iz, fz);
+    if (f.interp_ref) {
+        float t = fx;
+        fx = fz;
+        fz = t;
+    }
+    const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
+    const float a00 = gy * gz, a10 = fy * gz, a01 = gy * fz, a11 = fy * fz;
+    w[0] = gx * a00; w[1] = fx * a00; w[2] = gx * a10; w[3] = fx * a10;
+    w[4] = gx * a01; w[5] = fx * a01; w[6] = gx * a11; w[7] = fx * a11;
+    return (uint32_t)ix + (uint32_t)f.nx * iy + (uint32_t)f.nx * f.ny * iz;
+}
+
+// Trilinear E and B from the node-interleaved grid: the eight corner weights
+// once, then per pair of components one multiply and seven packed FMAs, in
+// corner order (each component's products and sums are those of a scalar
+// loop).
+__device__ __forceinline__ void trilinear_eb(const MixField& f, const uint64_t X[3], CellCacheEB& cc,
+                                             float E[3], float B[3])
+{
+    float w[8];
+    const uint32_t base = cell_and_weights(f, X, w);
+    if (base != cc.key) {
+        const uint32_t nx = f.nx, nxy = (uint32_t)f.nx * f.ny;
+        const float4* p = f.eb + (size_t)base * 2;
+        const uint32_t off[8] = {0, 1, nx, nx + 1, nxy, nxy + 1, nxy + nx, nxy + nx + 1};
+#pragma unroll
+        for (int k = 0; k < 8; k++) ld_node32(p + (size_t)off[k] * 2, cc.c[k][0], cc.c[k][1], cc.c[k][2]);
+        cc.key = base;
+    }
+    uint64_t wp = pack_f2(w[0], w[0]);
+    uint64_t r0 = mul_f2(wp, cc.c[0][0]), r1 = mul_f2(wp, cc.c[0][1]), r2 = mul_f2(wp, cc.c[0][2]);
+#pragma unroll
+    for (int k = 1; k < 8; k++) {
+        wp = pack_f2(w[k], w[k]);
+        r0 = fma_f2(wp, cc.c[k][0], r0);
+        r1 = fma_f2(wp, cc.c[k][1], r1);
+        r2 = fma_f2(wp, cc.c[k][2], r2);
+    }
+    unpack_f2(r0, E[0], E[1]);
+    unpack_f2(r1, E[2], B[0]);
+    unpack_f2(r2, B[1], B[2]);
+}
 
 // trilinear interpolation of a node-interleaved field with `stride` float4s per node
 template <int STRIDE>
@@ -113,12 +176,6 @@ __device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __r
     const uint32_t base = ix + nx * iy + nxy * iz;
     if (base != cc.key) {
         const float4* p = g + (size_t)base * STRIDE;
-        if constexpr (STRIDE == 2) {
-            // one 32-byte load per corner node ({E,0},{B,0}; nodes are 32-byte aligned)
-            const uint32_t off[8] = {0, 1, nx, nx + 1, nxy, nxy + 1, nxy + nx, nxy + nx + 1};
-#pragma unroll
-            for (int k = 0; k < 8; k++) ld_node32(p + (size_t)off[k] * 2, cc.c[2 * k], cc.c[2 * k + 1]);
-        } else
 #pragma unroll
         for (int c = 0; c < STRIDE; c++) {
             cc.c[0 * STRIDE + c] = __ldg(p + c);
@@ -160,7 +217,7 @@ __device__ __forceinline__ void trilinear_f(const MixField& f, const float4* __r
 
 // Per-particle register state of the field evaluation.
 struct FieldCache {
-    CellCache<2> eb;   // gridded E, B
+    CellCacheEB eb;    // gridded E, B
     CellCache<1> v;    // ABC velocity grid
 };
 
@@ -193,10 +250,7 @@ __device__ __forceinline__ void field_mixed(const MixField& f, const uint64_t X[
             E[2] = B[0] * v.y - B[1] * v.x;
         }
     } else if (SYS == TP_SYS_PIC) {
-        float4 eb[2];
-        trilinear_f<2>(f, f.eb, X, fc.eb, eb);
-        E[0] = eb[0].x; E[1] = eb[0].y; E[2] = eb[0].z;
-        B[0] = eb[1].x; B[1] = eb[1].y; B[2] = eb[1].z;
+        trilinear_eb(f, X, fc.eb, E, B);
     } else if (SYS == TP_SYS_MODESUM) {
         const uint32_t X32 = (uint32_t)(X[0] >> 32), Y32 = (uint32_t)(X[1] >> 32),
                        Z32 = (uint32_t)(X[2] >> 32);

@@ -28,7 +28,10 @@ __device__ __forceinline__ double pitch_mu(const MixField& f, const uint64_t X[3
     field_mixed<SYS>(f, X, E, B, smodes, fc);
     float bb = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
     float uu = sqrtf(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
-    return (double)((B[0] * u[0] + B[1] * u[1] + B[2] * u[2]) / (bb * uu));
+    // FP32 rounding can carry a cosine of u nearly along B just past +-1,
+    // where its arc cosine (the pitch angle) would be NaN: clamp it
+    const float c = (B[0] * u[0] + B[1] * u[1] + B[2] * u[2]) / (bb * uu);
+    return (double)fminf(1.0f, fmaxf(-1.0f, c));
 }
 
 // Persistent fixed-step tracking in mixed precision: the same schedule and
@@ -38,13 +41,20 @@ __device__ __forceinline__ double pitch_mu(const MixField& f, const uint64_t X[3
 // the initial state, its pitch cosine, the start time and the last diffusion
 // singles -- lives in shared memory, [row][thread], so the step loop keeps
 // only the push state and the cell cache in registers.
-enum : int { DG_SG = 0, DG_X0 = 8, DG_U0 = 11, DG_T0 = 14, DG_MU0 = 15, DG_ROWS = 16 };
+enum : int { DG_SG = 0, DG_X0 = 8, DG_U0 = 11, DG_T0 = 14, DG_MU0 = 15, DG_G0 = 16, DG_ROWS = 17 };
+
+// Resident blocks of 128 threads per SM the gridded kernel is compiled for
+// (its registers: 4 blocks allow 128 a thread).
+#ifndef TP_MIXED_PIC_MINBLOCKS
+#define TP_MIXED_PIC_MINBLOCKS 4
+#endif
 
 // Persistent fixed-step tracking in mixed precision: the same schedule and
 // diagnostics as the FP64 kernel (src/tracking.c:297-462); the mode table of
 // the plane-wave field is staged once per block in shared memory.
 template <int SYS>
-__global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, TrackBufs b, TrackParams q)
+__global__ void __launch_bounds__(kBlock, SYS == TP_SYS_PIC ? TP_MIXED_PIC_MINBLOCKS : 4)
+    track_mixed_kernel(MixField f, TrackBufs b, TrackParams q)
 {
     __shared__ double red[(kBlock / 32) * 8];
     __shared__ unsigned int hist[kMaxSmemBins];
@@ -85,6 +95,7 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
                 dg[DG_U0 + k][tx] = u0[k];
             }
             p.u[0] = (float)b.ux[i]; p.u[1] = (float)b.uy[i]; p.u[2] = (float)b.uz[i];
+            dg[DG_G0][tx] = sqrt(1.0 + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
             // mu of the initial state: the field at the initial position is static
             uint64_t X0[3];
             float uf0[3] = {(float)u0[0], (float)u0[1], (float)u0[2]};
@@ -134,9 +145,11 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
                 nst += 1;
                 done += 1;
                 if (esc_after == 0 && at_diff) {
-                    // calc_diff_coeff, src/diagnostics.c:659-705, FP64 accumulation
+                    // calc_diff_coeff, src/diagnostics.c:659-705, FP64 accumulation;
+                    // one FP64 reciprocal of 2t + dt instead of eight divisions
+                    // (the FP64 pipe runs at a small fraction of the FP32 rate)
                     double t = dg[DG_T0][tx] + done * q.dt;
-                    double tt = t * 2 + q.dt;
+                    double itt = 1.0 / (t * 2 + q.dt);
                     double dd[3];
 #pragma unroll
                     for (int k = 0; k < 3; k++) {
@@ -145,19 +158,19 @@ __global__ void __launch_bounds__(kBlock, 4) track_mixed_kernel(MixField f, Trac
                     }
                     const double u00 = dg[DG_U0][tx], u01 = dg[DG_U0 + 1][tx], u02 = dg[DG_U0 + 2][tx];
                     const double mu0 = dg[DG_MU0][tx];
-                    double dxx = dd[0] * dd[0] / tt, dyy = dd[1] * dd[1] / tt, dzz = dd[2] * dd[2] / tt;
+                    double dxx = dd[0] * dd[0] * itt, dyy = dd[1] * dd[1] * itt, dzz = dd[2] * dd[2] * itt;
                     double du0 = u00 - p.u[0], du1 = u01 - p.u[1], du2 = u02 - p.u[2];
                     double g1 = sqrt(1.0 + (double)p.u[0] * p.u[0] + (double)p.u[1] * p.u[1] + (double)p.u[2] * p.u[2]);
-                    double g0 = sqrt(1.0 + u00 * u00 + u01 * u01 + u02 * u02);
+                    double g0 = dg[DG_G0][tx];
                     double mu = pitch_mu<SYS>(f, p.X, p.u, smodes, fc);
                     double th = (double)acosf((float)mu) * (180.0 / 3.14159265358979323846);
                     double th0 = (double)acosf((float)mu0) * (180.0 / 3.14159265358979323846);
                     dg[DG_SG + 1][tx] = dxx; dg[DG_SG + 2][tx] = dyy; dg[DG_SG + 3][tx] = dzz;
                     dg[DG_SG + 0][tx] = dxx + dyy + dzz;
-                    dg[DG_SG + 4][tx] = (du0 * du0 + du1 * du1 + du2 * du2) / tt;
-                    dg[DG_SG + 5][tx] = (mu - mu0) * (mu - mu0) / tt;
-                    dg[DG_SG + 6][tx] = (th - th0) * (th - th0) / tt;
-                    dg[DG_SG + 7][tx] = (g1 - g0) * (g1 - g0) / tt;
+                    dg[DG_SG + 4][tx] = (du0 * du0 + du1 * du1 + du2 * du2) * itt;
+                    dg[DG_SG + 5][tx] = (mu - mu0) * (mu - mu0) * itt;
+                    dg[DG_SG + 6][tx] = (th - th0) * (th - th0) * itt;
+                    dg[DG_SG + 7][tx] = (g1 - g0) * (g1 - g0) * itt;
                 }
             }
             if (active && esc_pre == 0 && esc_after == 1 && f.bc_flag == 1 && ntp < q.nt_out)
@@ -310,15 +323,15 @@ int track_max_blocks_per_sm(int system_type, int nmodes)
     return e == cudaSuccess ? nb : 0;
 }
 
-// Interleaved node layout for the gathers: per node {Ex,Ey,Ez,0},{Bx,By,Bz,0}
+// Interleaved node layout for the gathers: per node {Ex,Ey,Ez,Bx,By,Bz,0,0}
 // (32 bytes, one sector) built from the reference's AoS float E and B arrays.
 __global__ void interleave_kernel(const float* __restrict__ e, const float* __restrict__ bf,
                                   size_t n, float4* __restrict__ eb)
 {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    eb[2 * i] = make_float4(e ? e[3 * i] : 0.f, e ? e[3 * i + 1] : 0.f, e ? e[3 * i + 2] : 0.f, 0.f);
-    eb[2 * i + 1] = make_float4(bf[3 * i], bf[3 * i + 1], bf[3 * i + 2], 0.f);
+    eb[2 * i] = make_float4(e ? e[3 * i] : 0.f, e ? e[3 * i + 1] : 0.f, e ? e[3 * i + 2] : 0.f, bf[3 * i]);
+    eb[2 * i + 1] = make_float4(bf[3 * i + 1], bf[3 * i + 2], 0.f, 0.f);
 }
 
 cudaError_t launch_interleave(const float* e, const float* bf, size_t n, float4* eb, cudaStream_t s)

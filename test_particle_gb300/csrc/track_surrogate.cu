@@ -466,7 +466,9 @@ __global__ void __launch_bounds__(kThreads, 1) track_surrogate_kernel(mixed::Mix
             float uf0[3] = {(float)u0[0], (float)u0[1], (float)u0[2]};
             float bb = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
             float uu = sqrtf(uf0[0] * uf0[0] + uf0[1] * uf0[1] + uf0[2] * uf0[2]);
-            mu0 = (double)((B[0] * uf0[0] + B[1] * uf0[1] + B[2] * uf0[2]) / (bb * uu));
+            // clamped to [-1, 1]: FP32 rounding can carry it just past, where
+            // the pitch angle's arc cosine would be NaN
+            mu0 = (double)fminf(1.0f, fmaxf(-1.0f, (B[0] * uf0[0] + B[1] * uf0[1] + B[2] * uf0[2]) / (bb * uu)));
         }
         int esc_pre = esc ? 1 : 0;
         int esc_after = esc_pre;
@@ -512,7 +514,7 @@ __global__ void __launch_bounds__(kThreads, 1) track_surrogate_kernel(mixed::Mix
                     double g0 = sqrt(1.0 + u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
                     float bb = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
                     float uu = sqrtf(p.u[0] * p.u[0] + p.u[1] * p.u[1] + p.u[2] * p.u[2]);
-                    double mu = (double)((B[0] * p.u[0] + B[1] * p.u[1] + B[2] * p.u[2]) / (bb * uu));
+                    double mu = (double)fminf(1.0f, fmaxf(-1.0f, (B[0] * p.u[0] + B[1] * p.u[1] + B[2] * p.u[2]) / (bb * uu)));
                     double th = (double)acosf((float)mu) * (180.0 / 3.14159265358979323846);
                     double th0 = (double)acosf((float)mu0) * (180.0 / 3.14159265358979323846);
                     sg[1] = dxx; sg[2] = dyy; sg[3] = dzz;

@@ -71,6 +71,7 @@ def test_modesum_fp64_is_periodic_and_has_the_stated_rms():
     dB/B0 = 1 (sum of a^2 / 2 over modes = 1)."""
     modes, f = _modesum_setup()
     xyzt = _points(4096, 2, 0.0, 1.0)
+    xyzt[:, :3] = np.floor(xyzt[:, :3] * 2.0 ** 30) / 2.0 ** 30  # dyadic: whole shifts are exact
     a = tp.get_emf(xyzt)
     sh = xyzt.copy()
     sh[:, :3] += np.array([3.0, -2.0, 5.0])

@@ -85,34 +85,57 @@ def fp32_rounded(p0):
     return p
 
 
+def sampling_floor(frames):
+    """Per frame, the expected L1 distance of two independent ensembles of
+    this size drawn from the spectrum: sum over bins of sqrt(4 p (1-p) / (pi N))."""
+    out = []
+    for fb in frames:
+        nb = fb.sum()
+        q = fb / nb
+        out.append(np.sqrt(4 * q * (1 - q) / (np.pi * nb)).sum())
+    return np.array(out)
+
+
 @pytest.mark.parametrize("kind", ["abc", "grid", "modesum"])
 def test_mixed_long_horizon_statistics(kind):
-    """Ensemble statistics over 2000 steps, 8192 particles.  The floor is the
-    FP64 path started from the initial state rounded to FP32 (the mixed path
-    keeps momenta in FP32): by chaos that FP64 run drifts away from the FP64
-    run as fast as the mixed run does.  Per output frame the mixed path's
-    spectrum L1 distance to FP64 must stay within 1.5x the floor's plus 3
-    sigma of the L1 statistic; per diffusion coefficient its largest row error
-    within max(1 %, 2x the floor's largest row error)."""
-    cfg, p0 = setup(kind, 2000)
+    """Ensemble statistics over 2000 steps, 65,536 particles, against the FP64
+    path from the same initial state.
+
+    Spectra, per output frame: the mixed path's L1 distance to FP64 must stay
+    within max(1.5 x the chaos floor, the sampling floor) + 3 sigma.  The chaos
+    floor is the distance of the FP64 run started from the initial state
+    rounded to FP32 (the mixed path keeps momenta in FP32); the mixed path,
+    which rounds at every step rather than once, decorrelates from FP64 about
+    one frame sooner, after which both sit at the sampling floor, the distance
+    of two independent ensembles of this size from the same distribution.  A
+    bias of the mixed path larger than that sampling noise fails the test.
+
+    Diffusion coefficients, per coefficient, largest relative error over the
+    rows: within max(1 %, 2 x the chaos floor's, 4 sigma), sigma = 2 / sqrt(N),
+    the relative standard deviation of the difference of two independent
+    ensemble means of squared Gaussian displacements (each sqrt(2 / N))."""
+    n = 65536
+    cfg, p0 = setup(kind, 2000, n=n)
     a = tp.track(p0, cfg["dt"], 4, 200, precision=tp.PREC_FP64)
     r = tp.track(fp32_rounded(p0), cfg["dt"], 4, 200, precision=tp.PREC_FP64)
     b = tp.track(p0, cfg["dt"], 4, 200, precision=tp.PREC_MIXED)
-    n = len(p0)
     assert b["espect"].sum() == a["espect"].sum() == 4 * n
     l1_mixed = _l1_frames(b["espect"], a["espect"], n)
-    l1_floor = _l1_frames(r["espect"], a["espect"], n)
-    print("%s L1 mixed %s floor %s 3sigma %.4f" % (kind, l1_mixed, l1_floor, 3 * sigma_l1(n)))
-    assert np.all(l1_mixed <= 1.5 * l1_floor + 3 * sigma_l1(n)), (l1_mixed, l1_floor)
+    l1_chaos = _l1_frames(r["espect"], a["espect"], n)
+    floor = sampling_floor(a["espect"])
+    bound = np.maximum(1.5 * l1_chaos, floor) + 3 * sigma_l1(n)
+    print("%s L1 mixed %s chaos %s sampling %s" % (kind, l1_mixed, l1_chaos, floor))
+    assert np.all(l1_mixed <= bound), (l1_mixed, bound)
     ref = a["dsum"][:, 1:]
     scale = np.abs(ref).max(axis=1)
     live = scale > 1e-12 * np.abs(ref).max()  # dee with E = 0 is rounding noise in every path
+    sig = 2.0 / np.sqrt(n)
     for c in np.nonzero(live)[0]:
         den = np.maximum(np.abs(ref[c]), 1e-300)
         em = np.max(np.abs(b["dsum"][c, 1:] - ref[c]) / den)
         ef = np.max(np.abs(r["dsum"][c, 1:] - ref[c]) / den)
-        print("%s diffusion row %d: mixed %.3e floor %.3e" % (kind, c, em, ef))
-        assert em <= max(0.01, 2.0 * ef), (c, em, ef)
+        print("%s diffusion row %d: mixed %.3e chaos %.3e" % (kind, c, em, ef))
+        assert np.isfinite(em) and em <= max(0.01, 2.0 * ef, 4 * sig), (c, em, ef)
     assert tp.device_status() == 0
 
 

@@ -68,9 +68,9 @@ def _case(kind, steps=300, n=4096, seed=21):
         mb = wl.kolmogorov_modes(64, 1, 8, 0.5, seed)
         mv = wl.kolmogorov_modes(64, 1, 8, 0.1, seed + 1)
         he, hb = tp.synth_pic_fields(mb, mv, 1.0, to_host=True)
-        g = np.zeros((len(he), 8), dtype=np.float32)
+        g = np.zeros((len(he), 8), dtype=np.float32)  # per node {Ex,Ey,Ez,Bx,By,Bz,0,0}
         g[:, 0:3] = he
-        g[:, 4:7] = hb
+        g[:, 3:6] = hb
         grid = torch.from_numpy(g).cuda()
         a.system_type, a.bc_flag = tp.SYS_PIC, 1
         a.nx = a.ny = a.nz = ng
