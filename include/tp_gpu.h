@@ -292,6 +292,11 @@ int tp_set_wait_limit(unsigned int polls);
  * D[128][n]; n a multiple of 16 in [16, 256], k a multiple of 64 in
  * [64, 256].  A self-check of the tensor-core path of the learned field model. */
 int tp_tc_gemm_bf16(int n, int k, const unsigned short *a, const unsigned short *b, float *d);
+/* D = A * B^T through the learned field model's training GEMM kernel
+ * (tcgen05.mma over a ring of k-atoms, FP32 accumulation in tensor memory):
+ * A[m][k], B[n][k] raw BF16, D[m][n] FP32; m a multiple of 128, n a multiple
+ * of 16 in [16, 256], k a multiple of 64.  A self-check of the training path. */
+int tp_tc_gemm_train_bf16(int m, int n, int k, const unsigned short *a, const unsigned short *b, float *d);
 
 /* Field lines of the gridded B (system types 3 and 4) from n seeds [n][3],
  * RK4 steps of length `step` on the unit vector of B, up to length_max in

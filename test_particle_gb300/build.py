@@ -34,6 +34,7 @@ UNITS = [
     ("host_config.o", "host_config.cpp", ["-x", "cu"]),
     ("noalloc.o", "noalloc.cu", []),
     ("tc_gemm.o", "tc_gemm.cu", []),
+    ("tc_train.o", "tc_train.cu", []),
     ("poincare.o", "poincare.cu", []),
     ("loaders.o", "loaders.cu", []),
 ]

@@ -1,12 +1,15 @@
 // mlp.cu -- training and inference of the learned field model on the tensor
-// cores: a tiled BF16 GEMM (mma.sync m16n8k16, FP32 accumulation) with fused
-// bias/SiLU epilogues, Fourier features, MSE loss, AdamW.
+// cores: the forward, data-gradient and weight-gradient GEMMs on tcgen05
+// (tc_train.cu, FP32 accumulation in tensor memory, fused bias / SiLU /
+// SiLU-derivative epilogues), Fourier features, MSE loss, AdamW.  A small
+// mma.sync GEMM remains for the output layer's 6 x 256 weight gradient.
 //
 // The model maps a position u in the periodic box (u = (x - min) / L) to the
 // six field components: 64 integer-lattice frequencies f_j give the features
 // sin(2 pi f_j . u), cos(2 pi f_j . u) (exact phases in 32-bit fixed point),
 // then 128 -> 256 -> 256 -> 256 -> 256 -> 6 with SiLU.  Outputs are trained
 // on normalised components (zero mean, unit variance per component).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -14,6 +17,7 @@
 
 #include "../../include/tp_gpu.h"
 #include "mlp_common.cuh"
+#include "tc_train.cuh"
 #include "tp_internal.h"
 #include "tp_mixed.cuh"
 
@@ -124,56 +128,6 @@ __global__ void __launch_bounds__(256) gemm_kernel(const __nv_bfloat16* __restri
         }
 }
 
-// z = acc + b; Z <- bf16(z) (kept for the backward pass), H <- bf16(silu(z))
-struct EpiHidden {
-    const float* b;
-    __nv_bfloat16* Z;
-    __nv_bfloat16* H;
-    int ld;
-    __device__ void operator()(int m, int n, float v0, float v1, int M, int N) const
-    {
-        if (m >= M) return;
-        if (n < N) {
-            float z = v0 + b[n];
-            Z[(size_t)m * ld + n] = __float2bfloat16(z);
-            H[(size_t)m * ld + n] = __float2bfloat16(silu(z));
-        }
-        if (n + 1 < N) {
-            float z = v1 + b[n + 1];
-            Z[(size_t)m * ld + n + 1] = __float2bfloat16(z);
-            H[(size_t)m * ld + n + 1] = __float2bfloat16(silu(z));
-        }
-    }
-};
-
-// y = acc + b (FP32 output layer)
-struct EpiOut {
-    const float* b;
-    float* Y;
-    int ld;
-    __device__ void operator()(int m, int n, float v0, float v1, int M, int N) const
-    {
-        if (m >= M) return;
-        if (n < N) Y[(size_t)m * ld + n] = v0 + b[n];
-        if (n + 1 < N) Y[(size_t)m * ld + n + 1] = v1 + b[n + 1];
-    }
-};
-
-// dZ = dH * silu'(Z), stored BF16
-struct EpiBackSilu {
-    const __nv_bfloat16* Z;
-    __nv_bfloat16* G;
-    int ld;
-    __device__ void operator()(int m, int n, float v0, float v1, int M, int N) const
-    {
-        if (m >= M) return;
-        if (n < N) G[(size_t)m * ld + n] = __float2bfloat16(v0 * silu_grad(__bfloat162float(Z[(size_t)m * ld + n])));
-        if (n + 1 < N)
-            G[(size_t)m * ld + n + 1] =
-                __float2bfloat16(v1 * silu_grad(__bfloat162float(Z[(size_t)m * ld + n + 1])));
-    }
-};
-
 // FP32 accumulation of a split-K weight gradient
 struct EpiAtomic {
     float* W;
@@ -213,15 +167,19 @@ __device__ __forceinline__ void features_row(const int* freq, uint32_t U0, uint3
     }
 }
 
+// X [n][128]; with XT, also transposed [128][n] (the weight-gradient operand)
 __global__ void features_kernel(const uint32_t* __restrict__ U, int n, const int* __restrict__ freq,
-                                __nv_bfloat16* __restrict__ X)
+                                __nv_bfloat16* __restrict__ X, __nv_bfloat16* __restrict__ XT = nullptr)
 {
     __shared__ int fs[3 * kFeat];
     for (int k = threadIdx.x; k < 3 * kFeat; k += blockDim.x) fs[k] = freq[k];
     __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    features_row(fs, U[3 * i], U[3 * i + 1], U[3 * i + 2], X + (size_t)i * kIn);
+    __nv_bfloat16* row = X + (size_t)i * kIn;
+    features_row(fs, U[3 * i], U[3 * i + 1], U[3 * i + 2], row);
+    if (XT)
+        for (int j = 0; j < kIn; j++) XT[(size_t)j * n + i] = row[j];
 }
 
 // ---------------------------------------------------------------- samples
@@ -265,7 +223,10 @@ __global__ void samples_kernel(uint64_t seed, long long first, int n, const tp_m
 }
 
 // ---------------------------------------------------------------- loss, biases, AdamW
-// dY = 2 (y - t_n) / (n * 6) with t_n the normalised target; BF16 dY padded to 16 columns
+// dY = 2 (y - t_n) / (n * 6) with t_n the normalised target; BF16 dY padded with
+// zeros to kDYld columns (one k-atom of the output layer's data-gradient GEMM)
+constexpr int kDYld = 64;
+constexpr int kWgradSplits = 80;  // most split-K parts of a weight-gradient GEMM
 __global__ void loss_kernel(const float* __restrict__ Y, const float* __restrict__ T, int n,
                             const float* __restrict__ mean, const float* __restrict__ istd,
                             __nv_bfloat16* __restrict__ dY, float* __restrict__ dYf,
@@ -275,7 +236,7 @@ __global__ void loss_kernel(const float* __restrict__ Y, const float* __restrict
     float l = 0.f;
     if (i < n) {
         const float scale = 2.0f / ((float)n * kOut);
-        for (int c = 0; c < kOutPad; c++) {
+        for (int c = 0; c < kDYld; c++) {
             float g = 0.f;
             if (c < kOut) {
                 float r = Y[(size_t)i * kOut + c] - (T[(size_t)i * kOut + c] - mean[c]) * istd[c];
@@ -283,7 +244,7 @@ __global__ void loss_kernel(const float* __restrict__ Y, const float* __restrict
                 g = r * scale;
                 if (dYf) dYf[(size_t)i * kOut + c] = g;
             }
-            dY[(size_t)i * kOutPad + c] = __float2bfloat16(g);
+            dY[(size_t)i * kDYld + c] = __float2bfloat16(g);
         }
     }
     for (int off = 16; off > 0; off >>= 1) l += __shfl_down_sync(0xffffffffu, l, off);
@@ -341,6 +302,16 @@ __global__ void to_bf16_kernel(const float* __restrict__ w, int out, int out_pad
     if (wt) wt[(size_t)k * out_pad + o] = v;
 }
 
+// The output layer's weights transposed and padded to one k-atom: WT4 [256][64],
+// WT4[k][o] = W4[o][k] for o < kOut, zero beyond.
+__global__ void wt4_pad_kernel(const __nv_bfloat16* __restrict__ wt4, __nv_bfloat16* __restrict__ wt4p)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kHid * kDYld) return;
+    int k = i / kDYld, o = i % kDYld;
+    wt4p[i] = o < kOutPad ? wt4[(size_t)k * kOutPad + o] : __float2bfloat16(0.f);
+}
+
 }  // namespace mlp
 
 // ---------------------------------------------------------------- host model
@@ -354,6 +325,7 @@ struct MlpState {
     size_t woff[kLayers], boff[kLayers];
     float *p = nullptr, *gr = nullptr, *m = nullptr, *v = nullptr;
     __nv_bfloat16 *wb[kLayers] = {}, *wt[kLayers] = {};
+    __nv_bfloat16* wt4p = nullptr;          // [256][64] output weights transposed, padded
     unsigned char* wpack = nullptr;         // kPackBytes, tensor-core inference layout
     int* freq = nullptr;
     float out_mean[kOut] = {0}, out_std[kOut] = {1, 1, 1, 1, 1, 1};
@@ -364,7 +336,11 @@ struct MlpState {
     __nv_bfloat16* X = nullptr;             // [cap][128]
     __nv_bfloat16 *Z[4] = {}, *H[4] = {};   // [cap][256]
     __nv_bfloat16 *G0 = nullptr, *G1 = nullptr;  // [cap][256] backward scratch
-    __nv_bfloat16* dY = nullptr;            // [cap][16]
+    __nv_bfloat16* dY = nullptr;            // [cap][kDYld]
+    __nv_bfloat16* XT = nullptr;            // [128][n] features transposed
+    __nv_bfloat16* HT[4] = {};              // [256][n] activations transposed
+    __nv_bfloat16* GT = nullptr;            // [256][n] pre-activation gradient transposed
+    float* partial = nullptr;               // split-K partial weight gradients
     float* Y = nullptr;                     // [cap][6]
     float* dYf = nullptr;                   // [cap][6]
     double* loss = nullptr;
@@ -394,26 +370,33 @@ static bool mlp_alloc_params()
             return false;
     }
     return cuda_ok(cudaMalloc(&M.wpack, kPackBytes), "mlp wpack") &&
+           cuda_ok(cudaMalloc(&M.wt4p, sizeof(__nv_bfloat16) * kHid * kDYld), "mlp wt4p") &&
+           cuda_ok(cudaMalloc(&M.partial, sizeof(float) * (size_t)kWgradSplits * kHid * kHid), "mlp partial") &&
            cuda_ok(cudaMalloc(&M.freq, sizeof(int) * 3 * kFeat), "mlp freq") &&
            cuda_ok(cudaMalloc(&M.d_mean, sizeof(float) * kOut), "mlp mean") &&
            cuda_ok(cudaMalloc(&M.d_istd, sizeof(float) * kOut), "mlp std") &&
            cuda_ok(cudaMalloc(&M.loss, sizeof(double)), "mlp loss");
 }
 
+// workspaces for batches of up to n samples (rounded up to a whole 128-row tile)
 static bool mlp_reserve(int n)
 {
+    n = (n + 127) / 128 * 128;
     if (n <= M.cap) return true;
     auto fr = [](void* p) { if (p) cudaFree(p); };
-    fr(M.X); fr(M.G0); fr(M.G1); fr(M.dY); fr(M.Y); fr(M.dYf);
-    for (int l = 0; l < 4; l++) { fr(M.Z[l]); fr(M.H[l]); }
+    fr(M.X); fr(M.G0); fr(M.G1); fr(M.dY); fr(M.Y); fr(M.dYf); fr(M.XT); fr(M.GT);
+    for (int l = 0; l < 4; l++) { fr(M.Z[l]); fr(M.H[l]); fr(M.HT[l]); }
     size_t h = sizeof(__nv_bfloat16) * (size_t)n * kHid;
     bool ok = cuda_ok(cudaMalloc(&M.X, sizeof(__nv_bfloat16) * (size_t)n * kIn), "X") &&
+              cuda_ok(cudaMalloc(&M.XT, sizeof(__nv_bfloat16) * (size_t)n * kIn), "XT") &&
               cuda_ok(cudaMalloc(&M.G0, h), "G0") && cuda_ok(cudaMalloc(&M.G1, h), "G1") &&
-              cuda_ok(cudaMalloc(&M.dY, sizeof(__nv_bfloat16) * (size_t)n * kOutPad), "dY") &&
+              cuda_ok(cudaMalloc(&M.GT, h), "GT") &&
+              cuda_ok(cudaMalloc(&M.dY, sizeof(__nv_bfloat16) * (size_t)n * kDYld), "dY") &&
               cuda_ok(cudaMalloc(&M.Y, sizeof(float) * (size_t)n * kOut), "Y") &&
               cuda_ok(cudaMalloc(&M.dYf, sizeof(float) * (size_t)n * kOut), "dYf");
     for (int l = 0; l < 4 && ok; l++)
-        ok = cuda_ok(cudaMalloc(&M.Z[l], h), "Z") && cuda_ok(cudaMalloc(&M.H[l], h), "H");
+        ok = cuda_ok(cudaMalloc(&M.Z[l], h), "Z") && cuda_ok(cudaMalloc(&M.H[l], h), "H") &&
+             cuda_ok(cudaMalloc(&M.HT[l], h), "HT");
     if (ok) M.cap = n;
     return ok;
 }
@@ -426,6 +409,7 @@ static bool mlp_refresh_bf16()
         to_bf16_kernel<<<(e + 255) / 256, 256, 0, s>>>(M.p + M.woff[l], layer_out(l), layer_out_pad(l),
                                                        layer_in(l), M.wb[l], M.wt[l]);
     }
+    wt4_pad_kernel<<<(kHid * kDYld + 255) / 256, 256, 0, s>>>(M.wt[kLayers - 1], M.wt4p);
     if (!cuda_ok(pack_weights(M.wb, M.wpack, s), "pack weights")) return false;
     float istd[kOut];
     for (int c = 0; c < kOut; c++) istd[c] = 1.0f / M.out_std[c];
@@ -434,51 +418,60 @@ static bool mlp_refresh_bf16()
     return cuda_ok(cudaGetLastError(), "bf16 refresh");
 }
 
-// forward of n samples from features X: fills Z/H and Y (normalised outputs)
+// forward of n samples from features X (rows up to the next multiple of 128
+// are computed too and ignored): fills Z/H (and H transposed) and Y
+// (normalised outputs), on the tensor cores
 static bool mlp_forward(int n)
 {
     cudaStream_t s = g.stream;
+    const int np = (n + 127) / 128 * 128;
     const __nv_bfloat16* in = M.X;
     int ldin = kIn;
     for (int l = 0; l < 4; l++) {
-        EpiHidden e{M.p + M.boff[l], M.Z[l], M.H[l], kHid};
-        if (!cuda_ok(gemm<false, false>(in, ldin, M.wb[l], layer_in(l), n, kHid, layer_in(l), 1, e, s),
+        if (!cuda_ok(tctrain::forward_hidden(in, ldin, M.wb[l], layer_in(l), np, M.p + M.boff[l], M.Z[l],
+                                             M.H[l], M.HT[l], g.d_status, s),
                      "fwd gemm")) return false;
         in = M.H[l];
         ldin = kHid;
     }
-    EpiOut eo{M.p + M.boff[4], M.Y, kOut};
-    return cuda_ok(gemm<false, false>(in, kHid, M.wb[4], kHid, n, kOut, kHid, 1, eo, s), "out gemm");
+    return cuda_ok(tctrain::forward_out(in, M.wb[4], np, M.p + M.boff[4], M.Y, g.d_status, s), "out gemm");
 }
 
-// backward of n samples after mlp_forward and the loss kernel: fills M.gr
+// backward of n samples (a multiple of 128) after mlp_forward and the loss
+// kernel: fills M.gr.  Data gradients and the hidden layers' weight gradients
+// on the tensor cores; the output layer's 6 x 256 weight gradient on mma.sync.
 static bool mlp_backward(int n)
 {
     cudaStream_t s = g.stream;
     cudaMemsetAsync(M.gr, 0, sizeof(float) * M.nparam, s);
     const int split = n >= 8192 ? (n + 4095) / 4096 : 1;
-    // output layer: dW4 = dYᵀ H3, db4 = sum dY, dH3 = dY W4
+    // output layer: dW4 = dY^T H3, db4 = sum dY, dH3 = dY W4 (times silu'(Z3))
     {
         EpiAtomic ew{M.gr + M.woff[4], kHid};
-        if (!cuda_ok(gemm<true, true>(M.dY, kOutPad, M.H[3], kHid, kOut, kHid, n, split, ew, s), "dW4"))
+        if (!cuda_ok(gemm<true, true>(M.dY, kDYld, M.H[3], kHid, kOut, kHid, n, split, ew, s), "dW4"))
             return false;
         bias_grad_f32_kernel<<<256, 32, 0, s>>>(M.dYf, n, kOut, M.gr + M.boff[4]);
-        EpiBackSilu eb{M.Z[3], M.G0, kHid};
-        if (!cuda_ok(gemm<false, false>(M.dY, kOutPad, M.wt[4], kOutPad, n, kHid, kOutPad, 1, eb, s), "dH3"))
+        if (!cuda_ok(tctrain::backward_data(M.dY, kDYld, M.wt4p, kDYld, n, M.Z[3], M.G0, M.GT, g.d_status, s),
+                     "dH3"))
             return false;
     }
     __nv_bfloat16 *gcur = M.G0, *gnext = M.G1;
     for (int l = 3; l >= 0; l--) {
-        const __nv_bfloat16* xin = l == 0 ? M.X : M.H[l - 1];
-        int kin = layer_in(l);
-        EpiAtomic ew{M.gr + M.woff[l], kin};
-        if (!cuda_ok(gemm<true, true>(gcur, kHid, xin, kin, kHid, kin, n, split, ew, s), "dW"))
+        const __nv_bfloat16* xt = l == 0 ? M.XT : M.HT[l - 1];
+        const int kin = layer_in(l);
+        // split K (the samples) so that the two 128-row tiles fill the SMs, at
+        // least four k-atoms per split
+        const int splits = std::max(1, std::min({kWgradSplits, 76, n / 256}));
+        if (!cuda_ok(tctrain::backward_weights(M.GT, xt, kin, n, M.partial, splits, M.gr + M.woff[l], g.d_status,
+                                               s),
+                     "dW"))
             return false;
         dim3 bg((kHid + 127) / 128, 64);
         bias_grad_kernel<<<bg, 128, 0, s>>>(gcur, n, kHid, kHid, M.gr + M.boff[l]);
         if (l > 0) {
-            EpiBackSilu eb{M.Z[l - 1], gnext, kHid};
-            if (!cuda_ok(gemm<false, false>(gcur, kHid, M.wt[l], kHid, n, kHid, kHid, 1, eb, s), "dH"))
+            if (!cuda_ok(tctrain::backward_data(gcur, kHid, M.wt[l], kHid, n, M.Z[l - 1], gnext, M.GT, g.d_status,
+                                                s),
+                         "dH"))
                 return false;
             __nv_bfloat16* tmp = gcur;
             gcur = gnext;
@@ -585,6 +578,10 @@ extern "C" int tp_mlp_get_weights(float* weights)
 extern "C" int tp_mlp_grad(int n, const unsigned int* u, const float* t, double* loss, float* y,
                            float* grads)
 {
+    if (n < 128 || n % 128) {
+        set_error(12, "tp_mlp_grad: n must be a positive multiple of 128");
+        return -1;
+    }
     if (!M.ready || !mlp_reserve(n)) return -1;
     cudaStream_t s = g.stream;
     uint32_t* dU;
@@ -593,7 +590,7 @@ extern "C" int tp_mlp_grad(int n, const unsigned int* u, const float* t, double*
         !cuda_ok(cudaMalloc(&dT, sizeof(float) * 6 * n), "t")) return -1;
     cudaMemcpyAsync(dU, u, sizeof(uint32_t) * 3 * n, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(dT, t, sizeof(float) * 6 * n, cudaMemcpyHostToDevice, s);
-    features_kernel<<<(n + 127) / 128, 128, 0, s>>>(dU, n, M.freq, M.X);
+    features_kernel<<<(n + 127) / 128, 128, 0, s>>>(dU, n, M.freq, M.X, M.XT);
     bool ok = mlp_forward(n) && mlp_loss(n, dT, loss) && mlp_backward(n);
     if (ok) {
         if (y) cudaMemcpyAsync(y, M.Y, sizeof(float) * 6 * n, cudaMemcpyDeviceToHost, s);
@@ -665,7 +662,7 @@ extern "C" int tp_mlp_train(long long nsamples, int batch, int epochs, double lr
     bool ok = mlp_refresh_bf16();
     for (long long it = 0; it < total && ok; it++) {
         long long bi = it % nb;
-        features_kernel<<<(batch + 127) / 128, 128, 0, s>>>(dU + 3 * bi * batch, batch, M.freq, M.X);
+        features_kernel<<<(batch + 127) / 128, 128, 0, s>>>(dU + 3 * bi * batch, batch, M.freq, M.X, M.XT);
         const bool last = it == total - 1;
         ok = mlp_forward(batch) && mlp_loss(batch, dT + 6 * bi * batch, last ? &loss : nullptr) &&
              mlp_backward(batch);

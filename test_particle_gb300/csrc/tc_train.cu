@@ -1,0 +1,349 @@
+// tc_train.cu -- the GEMMs of the learned field model's training on the
+// 5th-generation tensor cores: C[M][N] = sum_k A[m][k] B[n][k], both operands
+// BF16 and K-major in global memory (row-major with K contiguous), FP32
+// accumulation in tensor memory, and a fused epilogue per use (bias + SiLU of
+// the forward pass, the SiLU derivative of the backward pass, split-K
+// partial sums of the weight gradients).
+//
+// One CTA of 128 threads computes a 128 x N tile (N <= 256) over a range of
+// K: the K range streams through a ring of kRing shared-memory stages, one
+// k-atom (64 values of K) per stage, A (128 rows) and B (N rows) in the
+// 128-byte-swizzled K-major layout of tc_sm100.cuh.  Every thread copies its
+// share of a stage with 16-byte cp.async; once a stage has landed one thread
+// issues its four K = 16 MMAs (M = 128, N) and commits them to the stage's
+// mbarrier, which frees the stage for the copy kRing - 1 atoms ahead.  After
+// the last atom the four warps read their 32 accumulator lanes (rows) with
+// tcgen05.ld, 32 columns at a time, and hand them to the epilogue.  Every
+// mbarrier wait is bounded; a wait that runs out raises ST_TIMEOUT, the CTA
+// skips its stores, drains its MMAs (bounded) and frees its tensor memory.
+#include <cstdint>
+
+#include "../../include/tp_gpu.h"
+#include "mlp_common.cuh"
+#include "tc_sm100.cuh"
+#include "tc_train.cuh"
+#include "tp_internal.h"
+
+namespace tp {
+namespace tct {
+
+constexpr int kThreads = 128;
+constexpr int kRing = 4;
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+__host__ __device__ constexpr uint32_t a_stage_bytes() { return 128u * 128u; }
+__host__ __device__ constexpr uint32_t b_stage_bytes(int n) { return (uint32_t)n * 128u; }
+size_t smem_bytes(int n) { return 1024 + (size_t)kRing * (a_stage_bytes() + b_stage_bytes(n)); }
+
+// one k-atom of A (128 rows from m0) and B (n rows) into a stage
+__device__ __forceinline__ void load_stage(const __nv_bfloat16* __restrict__ A, int lda, int m0,
+                                           const __nv_bfloat16* __restrict__ B, int ldb, int n, int k0,
+                                           uint32_t sa, uint32_t sb)
+{
+    const int tid = threadIdx.x;
+    for (int c = tid; c < 128 * 8; c += kThreads) {
+        const int r = c >> 3, kk = (c & 7) * 8;
+        const __nv_bfloat16* src = A + (size_t)(m0 + r) * lda + k0 + kk;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa + tc::sw128_offset(128, r, kk)),
+                     "l"(src)
+                     : "memory");
+    }
+    for (int c = tid; c < n * 8; c += kThreads) {
+        const int r = c >> 3, kk = (c & 7) * 8;
+        const __nv_bfloat16* src = B + (size_t)r * ldb + k0 + kk;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sb + tc::sw128_offset(n, r, kk)),
+                     "l"(src)
+                     : "memory");
+    }
+}
+
+template <class Epi>
+__global__ void __launch_bounds__(kThreads, 1) tcgemm_kernel(const __nv_bfloat16* __restrict__ A, int lda,
+                                                             const __nv_bfloat16* __restrict__ B, int ldb,
+                                                             int N, int kchunk, int K, Epi epi,
+                                                             int* __restrict__ status)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bars[kRing + 1];
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.x * 128;
+    const int kbeg = blockIdx.y * kchunk, kend = min(K, kbeg + kchunk);
+    const int nk = (kend - kbeg) / 64;
+    const uint32_t raw = tc::smem_addr(smem_raw);
+    const uint32_t base = raw + ((1024u - (raw & 1023u)) & 1023u);
+    const uint32_t sa0 = base, sb0 = base + kRing * a_stage_bytes();
+    const uint32_t bar0 = tc::smem_addr(&bars[0]), done = tc::smem_addr(&bars[kRing]);
+    const uint32_t ncols = N <= 32 ? 32u : N <= 64 ? 64u : N <= 128 ? 128u : 256u;
+    if (tid == 0) {
+        for (int s = 0; s <= kRing; s++) tc::mbar_init(bar0 + 8 * s, 1);
+        tc::mbar_fence_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tc::smem_addr(&tmem_slot), ncols);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t idesc = tc::idesc_bf16_f32(128, N);
+    bool ok = true;
+    // prologue: the first kRing - 1 atoms
+    for (int s = 0; s < kRing - 1; s++) {
+        if (s < nk)
+            load_stage(A, lda, m0, B, ldb, N, kbeg + 64 * s, sa0 + s * a_stage_bytes(), sb0 + s * b_stage_bytes(N));
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    for (int kc = 0; kc < nk; kc++) {
+        const int s = kc % kRing;
+        asm volatile("cp.async.wait_group %0;" ::"n"(kRing - 2) : "memory");
+        tc::fence_async_smem();
+        __syncthreads();
+        if (tid == 0 && ok) {
+            tc::tc_fence_after();
+            const uint64_t ad = tc::desc_sw128(sa0 + s * a_stage_bytes());
+            const uint64_t bd = tc::desc_sw128(sb0 + s * b_stage_bytes(N));
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) tc::mma_bf16(tmem, ad + 2 * kk, bd + 2 * kk, idesc, (kc | kk) != 0);
+            tc::mma_commit(bar0 + 8 * s);
+        }
+        const int nxt = kc + kRing - 1;
+        if (nxt < nk) {
+            if (kc >= 1) {  // the stage's previous atom (kc - 1) must have been consumed
+                const int sp = (kc - 1) % kRing;
+                if (!tc::mbar_wait(bar0 + 8 * sp, (uint32_t)((kc - 1) / kRing) & 1u, kWaitLimit)) ok = false;
+            }
+            if (ok)
+                load_stage(A, lda, m0, B, ldb, N, kbeg + 64 * nxt, sa0 + (nxt % kRing) * a_stage_bytes(),
+                           sb0 + (nxt % kRing) * b_stage_bytes(N));
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    ok = __syncthreads_and(ok) != 0;
+    if (tid == 0) tc::mma_commit(done);
+    const bool fine = tc::mbar_wait(done, 0, kWaitLimit);
+    if (!(ok && fine) && (tid & 31) == 0) atomicOr(status, ST_TIMEOUT);
+    tc::tc_fence_after();
+    if (ok && fine && nk > 0) {
+        const int row = m0 + tid;
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        if (N >= 32) {
+            for (int c = 0; c < N; c += 32) {
+                float v[32];
+                tc::tmem_ld32(tmem + lane_base + (uint32_t)c, v);
+                epi(row, c, v, 32);
+            }
+        } else {
+            float v[32];
+            tc::tmem_ld16(tmem + lane_base, v);
+            epi(row, 0, v, 16);
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
+template <class Epi>
+static cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M, int N, int K,
+                          int splits, const Epi& epi, int* status, cudaStream_t s)
+{
+    if (M % 128 || N % 16 || N < 16 || N > 256 || K % 64 || K < 64 || splits < 1) return cudaErrorInvalidValue;
+    int kchunk = (K / 64 + splits - 1) / splits * 64;
+    splits = (K + kchunk - 1) / kchunk;
+    const size_t smem = smem_bytes(N);
+    cudaError_t e = cudaFuncSetAttribute(tcgemm_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(M / 128, splits);
+    tcgemm_kernel<Epi><<<grid, kThreads, smem, s>>>(A, lda, B, ldb, N, kchunk, K, epi, status);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- epilogues
+// Each gets 32 (or 16) consecutive columns c0.. of row m.
+struct EpiStoreF32 {  // D[m][n] = acc (self-check)
+    float* D;
+    int ld;
+    __device__ void operator()(int m, int c0, const float* v, int cnt) const
+    {
+        for (int i = 0; i < cnt; i++) D[(size_t)m * ld + c0 + i] = v[i];
+    }
+};
+
+// z = acc + b; Z, H = silu(z) row-major [M][256] and H transposed [256][M]
+struct EpiHiddenT {
+    const float* b;
+    __nv_bfloat16 *Z, *H, *HT;
+    int M;
+    __device__ void operator()(int m, int c0, const float* v, int cnt) const
+    {
+#pragma unroll
+        for (int i = 0; i < 32; i += 8) {
+            uint32_t zp[4], hp[4];
+#pragma unroll
+            for (int j = 0; j < 8; j += 2) {
+                const float z0 = v[i + j] + b[c0 + i + j], z1 = v[i + j + 1] + b[c0 + i + j + 1];
+                zp[j / 2] = mlp::pack_bf16(z0, z1);
+                hp[j / 2] = mlp::pack_bf16(mlp::silu(z0), mlp::silu(z1));
+            }
+            *reinterpret_cast<uint4*>(Z + (size_t)m * mlp::kHid + c0 + i) = make_uint4(zp[0], zp[1], zp[2], zp[3]);
+            *reinterpret_cast<uint4*>(H + (size_t)m * mlp::kHid + c0 + i) = make_uint4(hp[0], hp[1], hp[2], hp[3]);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const uint32_t w = hp[j / 2];
+                reinterpret_cast<unsigned short*>(HT)[(size_t)(c0 + i + j) * M + m] =
+                    (unsigned short)((j & 1) ? (w >> 16) : (w & 0xffffu));
+            }
+        }
+    }
+};
+
+// y = acc + b for the first kOut columns (FP32 [M][kOut])
+struct EpiOutT {
+    const float* b;
+    float* Y;
+    __device__ void operator()(int m, int c0, const float* v, int cnt) const
+    {
+        for (int c = 0; c < mlp::kOut; c++) Y[(size_t)m * mlp::kOut + c] = v[c] + b[c];
+    }
+};
+
+// g = acc * silu'(Z): G row-major [M][256] and transposed [256][M]
+struct EpiBackSiluT {
+    const __nv_bfloat16* Z;
+    __nv_bfloat16 *G, *GT;
+    int M;
+    __device__ void operator()(int m, int c0, const float* v, int cnt) const
+    {
+#pragma unroll
+        for (int i = 0; i < 32; i += 8) {
+            const uint4 zr = *reinterpret_cast<const uint4*>(Z + (size_t)m * mlp::kHid + c0 + i);
+            const uint32_t zw[4] = {zr.x, zr.y, zr.z, zr.w};
+            uint32_t gp[4];
+#pragma unroll
+            for (int j = 0; j < 8; j += 2) {
+                const __nv_bfloat162 z2 = *reinterpret_cast<const __nv_bfloat162*>(&zw[j / 2]);
+                const float g0 = v[i + j] * mlp::silu_grad(__low2float(z2));
+                const float g1 = v[i + j + 1] * mlp::silu_grad(__high2float(z2));
+                gp[j / 2] = mlp::pack_bf16(g0, g1);
+            }
+            *reinterpret_cast<uint4*>(G + (size_t)m * mlp::kHid + c0 + i) = make_uint4(gp[0], gp[1], gp[2], gp[3]);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const uint32_t w = gp[j / 2];
+                reinterpret_cast<unsigned short*>(GT)[(size_t)(c0 + i + j) * M + m] =
+                    (unsigned short)((j & 1) ? (w >> 16) : (w & 0xffffu));
+            }
+        }
+    }
+};
+
+// split-K partial of a weight gradient: P[split][m][n] (FP32)
+struct EpiPartial {
+    float* P;
+    int M, N;
+    __device__ void operator()(int m, int c0, const float* v, int cnt) const
+    {
+        float* dst = P + ((size_t)blockIdx.y * M + m) * N + c0;
+        for (int i = 0; i < cnt; i += 4)
+            *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+    }
+};
+
+// gr[m][n] (row length N) += sum over the splits of P[split][m][n]
+__global__ void reduce_partials_kernel(const float* __restrict__ P, int splits, int M, int N, float* __restrict__ gr)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M * N) return;
+    float s = 0.f;
+    for (int k = 0; k < splits; k++) s += P[(size_t)k * M * N + i];
+    gr[i] += s;
+}
+
+}  // namespace tct
+
+namespace tctrain {
+
+using namespace tct;
+
+cudaError_t forward_hidden(const __nv_bfloat16* X, int lda, const __nv_bfloat16* W, int kin, int M, const float* b,
+                           __nv_bfloat16* Z, __nv_bfloat16* H, __nv_bfloat16* HT, int* status, cudaStream_t s)
+{
+    return launch(X, lda, W, kin, M, mlp::kHid, kin, 1, EpiHiddenT{b, Z, H, HT, M}, status, s);
+}
+
+cudaError_t forward_out(const __nv_bfloat16* H3, const __nv_bfloat16* W4, int M, const float* b, float* Y,
+                        int* status, cudaStream_t s)
+{
+    return launch(H3, mlp::kHid, W4, mlp::kHid, M, mlp::kOutPad, mlp::kHid, 1, EpiOutT{b, Y}, status, s);
+}
+
+cudaError_t backward_data(const __nv_bfloat16* Gin, int ldg, const __nv_bfloat16* WT, int kout, int M,
+                          const __nv_bfloat16* Zprev, __nv_bfloat16* G, __nv_bfloat16* GT, int* status,
+                          cudaStream_t s)
+{
+    return launch(Gin, ldg, WT, kout, M, mlp::kHid, kout, 1, EpiBackSiluT{Zprev, G, GT, M}, status, s);
+}
+
+cudaError_t backward_weights(const __nv_bfloat16* GT, const __nv_bfloat16* XT, int kin, int nsamp, float* partial,
+                             int splits, float* gr, int* status, cudaStream_t s)
+{
+    // dW[256][kin] = G^T X: M = 256 output features, N = kin, K = samples
+    cudaError_t e = launch(GT, nsamp, XT, nsamp, mlp::kHid, kin, nsamp, splits,
+                           EpiPartial{partial, mlp::kHid, kin}, status, s);
+    if (e != cudaSuccess) return e;
+    const int kchunk = (nsamp / 64 + splits - 1) / splits * 64;
+    const int used = (nsamp + kchunk - 1) / kchunk;
+    const int tot = mlp::kHid * kin;
+    reduce_partials_kernel<<<(tot + 255) / 256, 256, 0, s>>>(partial, used, mlp::kHid, kin, gr);
+    return cudaGetLastError();
+}
+
+cudaError_t gemm_f32(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K, float* D, int* status,
+                     cudaStream_t s)
+{
+    return launch(A, K, B, K, M, N, K, 1, EpiStoreF32{D, N}, status, s);
+}
+
+}  // namespace tctrain
+}  // namespace tp
+
+using namespace tp;
+
+// D[m][n] = A[m][k] * B[n][k]^T with BF16 inputs (raw 16-bit patterns) and FP32
+// output, through the training GEMM kernel: m a multiple of 128, n a multiple
+// of 16 in [16, 256], k a multiple of 64.
+extern "C" int tp_tc_gemm_train_bf16(int m, int n, int k, const unsigned short* a, const unsigned short* b,
+                                     float* d)
+{
+    if (m < 128 || m % 128 || n < 16 || n > 256 || n % 16 || k < 64 || k % 64 || !a || !b || !d) {
+        set_error(6, "tp_tc_gemm_train_bf16: m a multiple of 128, n 16..256 in steps of 16, k a multiple of 64");
+        return -1;
+    }
+    if (!ensure_init()) return -1;
+    cudaStream_t s = g.stream;
+    const size_t sa = sizeof(uint16_t) * (size_t)m * k, sb = sizeof(uint16_t) * (size_t)n * k,
+                 sd = sizeof(float) * (size_t)m * n;
+    void *dA = nullptr, *dB = nullptr, *dD = nullptr;
+    bool ok = cuda_ok(cudaMalloc(&dA, sa), "A") && cuda_ok(cudaMalloc(&dB, sb), "B") &&
+              cuda_ok(cudaMalloc(&dD, sd), "D");
+    if (ok) {
+        cudaMemcpyAsync(dA, a, sa, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(dB, b, sb, cudaMemcpyHostToDevice, s);
+        cudaMemsetAsync(dD, 0, sd, s);
+        ok = cuda_ok(tctrain::gemm_f32(static_cast<const __nv_bfloat16*>(dA), static_cast<const __nv_bfloat16*>(dB),
+                                       m, n, k, static_cast<float*>(dD), g.d_status, s),
+                     "train gemm");
+    }
+    if (ok) {
+        cudaMemcpyAsync(d, dD, sd, cudaMemcpyDeviceToHost, s);
+        ok = cuda_ok(cudaStreamSynchronize(s), "train gemm sync");
+    }
+    if (dA) cudaFree(dA);
+    if (dB) cudaFree(dB);
+    if (dD) cudaFree(dD);
+    return ok ? 0 : -1;
+}

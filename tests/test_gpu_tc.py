@@ -36,3 +36,35 @@ def test_tile_gemm_matches_fp64(n, k):
     # FP32 accumulation of k products of BF16 values
     assert np.abs(d - ref).max() <= 1e-5 * np.abs(ref).max(), np.abs(d - ref).max()
     assert tp.device_status() == 0
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 256, 256), (256, 16, 256), (384, 128, 640), (256, 256, 64),
+                                   (128, 48, 4096)])
+def test_training_gemm_matches_fp64(m, n, k):
+    """The training GEMM kernel (ring of k-atoms through shared memory, one
+    tcgen05.mma chain per 128-row tile) over several tiles and long K."""
+    rng = np.random.default_rng(m * 7 + n * 1000 + k)
+    a = bf16_bits(rng.uniform(-1, 1, size=(m, k)))
+    b = bf16_bits(rng.uniform(-1, 1, size=(n, k)))
+    d = np.zeros((m, n), dtype=np.float32)
+    L = tp.lib()
+    L.tp_tc_gemm_train_bf16.restype = C.c_int
+    u16 = C.POINTER(C.c_uint16)
+    rc = L.tp_tc_gemm_train_bf16(m, n, k, a.ctypes.data_as(u16), b.ctypes.data_as(u16),
+                                 d.ctypes.data_as(C.POINTER(C.c_float)))
+    assert rc == 0
+    ref = bits_to_f64(a) @ bits_to_f64(b).T
+    # FP32 accumulation of k products of BF16 values: |error| <= k 2^-24 sum |a b|
+    bound = k * 2.0 ** -24 * (np.abs(bits_to_f64(a)) @ np.abs(bits_to_f64(b)).T)
+    assert np.all(np.abs(d - ref) <= bound + 1e-30), np.abs(d - ref).max()
+    assert tp.device_status() == 0
+
+
+def test_training_gemm_rejects_bad_shapes():
+    L = tp.lib()
+    L.tp_tc_gemm_train_bf16.restype = C.c_int
+    z = np.zeros(1, dtype=np.uint16).ctypes.data_as(C.POINTER(C.c_uint16))
+    d = np.zeros(1, dtype=np.float32).ctypes.data_as(C.POINTER(C.c_float))
+    for m, n, k in ((100, 16, 64), (128, 8, 64), (128, 272, 64), (128, 16, 96)):
+        assert L.tp_tc_gemm_train_bf16(m, n, k, z, z, d) != 0
+    tp.lib().tp_clear_status()
