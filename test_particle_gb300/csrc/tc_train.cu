@@ -130,10 +130,13 @@ __global__ void __launch_bounds__(kThreads, 1) tcgemm_kernel(const __nv_bfloat16
         const int row = m0 + tid;
         const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
         if (N >= 32) {
+            // 32 columns at a time; a last chunk of 16 (N an odd multiple of
+            // 16) reads 16 columns past N inside the allocation and hands on
+            // only the 16 that exist
             for (int c = 0; c < N; c += 32) {
                 float v[32];
                 tc::tmem_ld32(tmem + lane_base + (uint32_t)c, v);
-                epi(row, c, v, 32);
+                epi(row, c, v, min(32, N - c));
             }
         } else {
             float v[32];
