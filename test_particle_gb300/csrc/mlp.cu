@@ -1,8 +1,9 @@
-// mlp.cu -- training and inference of the learned field model on the tensor
-// cores: the forward, data-gradient and weight-gradient GEMMs on tcgen05
-// (tc_train.cu, FP32 accumulation in tensor memory, fused bias / SiLU /
-// SiLU-derivative epilogues), Fourier features, MSE loss, AdamW.  A small
-// mma.sync GEMM remains for the output layer's 6 x 256 weight gradient.
+// mlp.cu -- training and inference of the learned field model: the forward,
+// data-gradient and hidden weight-gradient GEMMs on the 5th-generation tensor
+// cores (tc_train.cu: tcgen05.mma, FP32 accumulation in tensor memory, fused
+// bias / SiLU / SiLU-derivative epilogues), Fourier features, MSE loss, the
+// bias gradients and the output layer's 6 x 256 weight gradient as
+// reductions on the CUDA cores, AdamW.
 //
 // The model maps a position u in the periodic box (u = (x - min) / L) to the
 // six field components: 64 integer-lattice frequencies f_j give the features
@@ -23,134 +24,6 @@
 
 namespace tp {
 namespace mlp {
-
-// ---------------------------------------------------------------- GEMM
-// C[m][n] = sum_k A(m, k) * B(n, k); A(m, k) = A[m * lda + k] (or A[k * lda + m]
-// with AT), B(n, k) = B[n * ldb + k] (or B[k * ldb + n] with BT).  Block tile
-// 128 x 128 x 32, 8 warps as 4 (m) x 2 (n), each warp 32 x 64.
-constexpr int TM = 128, TN = 128, TK = 32, TKP = TK + 8;
-
-template <bool AT, bool BT, class Epi>
-__global__ void __launch_bounds__(256) gemm_kernel(const __nv_bfloat16* __restrict__ A, int lda,
-                                                   const __nv_bfloat16* __restrict__ B, int ldb,
-                                                   int M, int N, int K, int kchunk, Epi epi)
-{
-    __shared__ __align__(16) __nv_bfloat16 As[TM][TKP];
-    __shared__ __align__(16) __nv_bfloat16 Bs[TN][TKP];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = warp & 3, wn = warp >> 2;
-    const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
-    const int kbeg = blockIdx.z * kchunk;
-    const int kend = min(K, kbeg + kchunk);
-    const int g = lane >> 2, t = lane & 3;
-    float acc[2][8][4];
-#pragma unroll
-    for (int i = 0; i < 2; i++)
-#pragma unroll
-        for (int j = 0; j < 8; j++)
-#pragma unroll
-            for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
-    const __nv_bfloat16 zero = __float2bfloat16(0.f);
-
-    for (int k0 = kbeg; k0 < kend; k0 += TK) {
-        // ---- stage A and B tiles (canonical [row][k] layouts)
-#pragma unroll
-        for (int r = 0; r < 2; r++) {
-            int c = tid + r * 256;  // 512 chunks of 8 elements
-            if (!AT) {
-                int row = c >> 2, kk = (c & 3) * 8;
-                int m = m0 + row;
-#pragma unroll
-                for (int e = 0; e < 8; e++) {
-                    int k = k0 + kk + e;
-                    As[row][kk + e] = (m < M && k < kend) ? A[(size_t)m * lda + k] : zero;
-                }
-            } else {
-                int kr = c >> 4, mm = (c & 15) * 8;
-                int k = k0 + kr;
-#pragma unroll
-                for (int e = 0; e < 8; e++) {
-                    int m = m0 + mm + e;
-                    As[mm + e][kr] = (m < M && k < kend) ? A[(size_t)k * lda + m] : zero;
-                }
-            }
-            if (!BT) {
-                int row = c >> 2, kk = (c & 3) * 8;
-                int n = n0 + row;
-#pragma unroll
-                for (int e = 0; e < 8; e++) {
-                    int k = k0 + kk + e;
-                    Bs[row][kk + e] = (n < N && k < kend) ? B[(size_t)n * ldb + k] : zero;
-                }
-            } else {
-                int kr = c >> 4, nn = (c & 15) * 8;
-                int k = k0 + kr;
-#pragma unroll
-                for (int e = 0; e < 8; e++) {
-                    int n = n0 + nn + e;
-                    Bs[nn + e][kr] = (n < N && k < kend) ? B[(size_t)k * ldb + n] : zero;
-                }
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int ks = 0; ks < TK; ks += 16) {
-            uint32_t af[2][4], bf[8][2];
-#pragma unroll
-            for (int i = 0; i < 2; i++) {
-                int r = wm * 32 + i * 16 + g;
-                af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t]);
-                af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t]);
-                af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t + 8]);
-                af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t + 8]);
-            }
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                int r = wn * 64 + j * 8 + g;
-                bf[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[r][ks + 2 * t]);
-                bf[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[r][ks + 2 * t + 8]);
-            }
-#pragma unroll
-            for (int i = 0; i < 2; i++)
-#pragma unroll
-                for (int j = 0; j < 8; j++) mma_bf16(acc[i][j], af[i], bf[j]);
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int i = 0; i < 2; i++)
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            int m = m0 + wm * 32 + i * 16 + g;
-            int n = n0 + wn * 64 + j * 8 + 2 * t;
-            epi(m, n, acc[i][j][0], acc[i][j][1], M, N);
-            epi(m + 8, n, acc[i][j][2], acc[i][j][3], M, N);
-        }
-}
-
-// FP32 accumulation of a split-K weight gradient
-struct EpiAtomic {
-    float* W;
-    int ld;
-    __device__ void operator()(int m, int n, float v0, float v1, int M, int N) const
-    {
-        if (m >= M) return;
-        if (n < N) atomicAdd(&W[(size_t)m * ld + n], v0);
-        if (n + 1 < N) atomicAdd(&W[(size_t)m * ld + n + 1], v1);
-    }
-};
-
-template <bool AT, bool BT, class Epi>
-static cudaError_t gemm(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M,
-                        int N, int K, int splits, Epi epi, cudaStream_t s)
-{
-    int kchunk = (K + splits - 1) / splits;
-    kchunk = (kchunk + TK - 1) / TK * TK;
-    splits = (K + kchunk - 1) / kchunk;
-    dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM, splits);
-    gemm_kernel<AT, BT, Epi><<<grid, 256, 0, s>>>(A, lda, B, ldb, M, N, K, kchunk, epi);
-    return cudaGetLastError();
-}
 
 // ---------------------------------------------------------------- features
 // X[b][j] = sin(2 pi f_j . u_b), X[b][64 + j] = cos(...); u as 32-bit fixed point
@@ -252,24 +125,56 @@ __global__ void loss_kernel(const float* __restrict__ Y, const float* __restrict
 }
 
 // db[c] += sum_rows G[row][c] (BF16 rows of width ld)
-__global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ G, int rows, int cols, int ld,
-                                 float* __restrict__ db)
+// db[c] += sum over the n samples of GT[c][*] (the gradient transposed, one row
+// per feature, so every block reads one contiguous row); one block per
+// feature, a fixed summation order.
+__global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ GT, int n, float* __restrict__ db)
 {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= cols) return;
+    __shared__ float red[8];
+    const __nv_bfloat162* row = reinterpret_cast<const __nv_bfloat162*>(GT + (size_t)blockIdx.x * n);
     float s = 0.f;
-    for (int r = blockIdx.y; r < rows; r += gridDim.y) s += __bfloat162float(G[(size_t)r * ld + c]);
-    atomicAdd(&db[c], s);
+    for (int i = threadIdx.x; i < n / 2; i += blockDim.x) {
+        const float2 v = __bfloat1622float2(row[i]);
+        s += v.x + v.y;
+    }
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        db[blockIdx.x] += t;
+    }
 }
 
-__global__ void bias_grad_f32_kernel(const float* __restrict__ G, int rows, int cols,
-                                     float* __restrict__ db)
+// The output layer's gradients from the FP32 loss gradient dYf [n][6] and the
+// last hidden activations H3 [n][256]: dW4[o][k] += sum_r dYf[r][o] H3[r][k],
+// db4[o] += sum_r dYf[r][o].  A block takes kOutRows consecutive samples:
+// thread k owns column k of H3 and keeps six sums; FP32 atomics add the
+// block's partial sums.
+constexpr int kOutRows = 512;
+__global__ void __launch_bounds__(256) out_grad_kernel(const float* __restrict__ dYf,
+                                                       const __nv_bfloat16* __restrict__ H3, int n,
+                                                       float* __restrict__ dW4, float* __restrict__ db4)
 {
-    int c = threadIdx.x;
-    if (c >= cols) return;
-    float s = 0.f;
-    for (int r = blockIdx.x; r < rows; r += gridDim.x) s += G[(size_t)r * cols + c];
-    atomicAdd(&db[c], s);
+    __shared__ float dy[kOutRows * kOut];
+    const int r0 = blockIdx.x * kOutRows, nr = min(kOutRows, n - r0);
+    for (int i = threadIdx.x; i < nr * kOut; i += blockDim.x) dy[i] = dYf[(size_t)r0 * kOut + i];
+    __syncthreads();
+    const int k = threadIdx.x;
+    float acc[kOut] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int r = 0; r < nr; r++) {
+        const float h = __bfloat162float(H3[(size_t)(r0 + r) * kHid + k]);
+#pragma unroll
+        for (int o = 0; o < kOut; o++) acc[o] = fmaf(dy[r * kOut + o], h, acc[o]);
+    }
+#pragma unroll
+    for (int o = 0; o < kOut; o++) atomicAdd(&dW4[o * kHid + k], acc[o]);
+    if (k < kOut) {
+        float t = 0.f;
+        for (int r = 0; r < nr; r++) t += dy[r * kOut + k];
+        atomicAdd(&db4[k], t);
+    }
 }
 
 struct Adam {
@@ -439,18 +344,16 @@ static bool mlp_forward(int n)
 
 // backward of n samples (a multiple of 128) after mlp_forward and the loss
 // kernel: fills M.gr.  Data gradients and the hidden layers' weight gradients
-// on the tensor cores; the output layer's 6 x 256 weight gradient on mma.sync.
+// on the tensor cores; bias gradients and the output layer's weight gradient
+// as reductions.
 static bool mlp_backward(int n)
 {
     cudaStream_t s = g.stream;
     cudaMemsetAsync(M.gr, 0, sizeof(float) * M.nparam, s);
-    const int split = n >= 8192 ? (n + 4095) / 4096 : 1;
     // output layer: dW4 = dY^T H3, db4 = sum dY, dH3 = dY W4 (times silu'(Z3))
     {
-        EpiAtomic ew{M.gr + M.woff[4], kHid};
-        if (!cuda_ok(gemm<true, true>(M.dY, kDYld, M.H[3], kHid, kOut, kHid, n, split, ew, s), "dW4"))
-            return false;
-        bias_grad_f32_kernel<<<256, 32, 0, s>>>(M.dYf, n, kOut, M.gr + M.boff[4]);
+        out_grad_kernel<<<(n + kOutRows - 1) / kOutRows, 256, 0, s>>>(M.dYf, M.H[3], n, M.gr + M.woff[4],
+                                                                       M.gr + M.boff[4]);
         if (!cuda_ok(tctrain::backward_data(M.dY, kDYld, M.wt4p, kDYld, n, M.Z[3], M.G0, M.GT, g.d_status, s),
                      "dH3"))
             return false;
@@ -466,8 +369,7 @@ static bool mlp_backward(int n)
                                                s),
                      "dW"))
             return false;
-        dim3 bg((kHid + 127) / 128, 64);
-        bias_grad_kernel<<<bg, 128, 0, s>>>(gcur, n, kHid, kHid, M.gr + M.boff[l]);
+        bias_grad_kernel<<<kHid, 256, 0, s>>>(M.GT, n, M.gr + M.boff[l]);
         if (l > 0) {
             if (!cuda_ok(tctrain::backward_data(gcur, kHid, M.wt[l], kHid, n, M.Z[l - 1], gnext, M.GT, g.d_status,
                                                 s),

@@ -6,16 +6,19 @@
 // partial sums of the weight gradients).
 //
 // One CTA of 128 threads computes a 128 x N tile (N <= 256) over a range of
-// K: the K range streams through a ring of kRing shared-memory stages, one
+// K: the K range streams through a ring of RING shared-memory stages, one
 // k-atom (64 values of K) per stage, A (128 rows) and B (N rows) in the
 // 128-byte-swizzled K-major layout of tc_sm100.cuh.  Every thread copies its
 // share of a stage with 16-byte cp.async; once a stage has landed one thread
 // issues its four K = 16 MMAs (M = 128, N) and commits them to the stage's
-// mbarrier, which frees the stage for the copy kRing - 1 atoms ahead.  After
+// mbarrier, which frees the stage for the copy RING - 1 atoms ahead.  After
 // the last atom the four warps read their 32 accumulator lanes (rows) with
 // tcgen05.ld, 32 columns at a time, and hand them to the epilogue.  Every
 // mbarrier wait is bounded; a wait that runs out raises ST_TIMEOUT, the CTA
 // skips its stores, drains its MMAs (bounded) and frees its tensor memory.
+// Long K ranges (the weight gradients) use 4 stages; short ones (K <= 256:
+// four atoms) use 2, which halves the shared memory so that two CTAs share
+// an SM and one's epilogue overlaps the other's copies and MMAs.
 #include <cstdint>
 
 #include "../../include/tp_gpu.h"
@@ -28,12 +31,12 @@ namespace tp {
 namespace tct {
 
 constexpr int kThreads = 128;
-constexpr int kRing = 4;
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 __host__ __device__ constexpr uint32_t a_stage_bytes() { return 128u * 128u; }
 __host__ __device__ constexpr uint32_t b_stage_bytes(int n) { return (uint32_t)n * 128u; }
-size_t smem_bytes(int n) { return 1024 + (size_t)kRing * (a_stage_bytes() + b_stage_bytes(n)); }
+__host__ __device__ constexpr int ring_for(int k_atoms) { return k_atoms <= 4 ? 2 : 4; }
+size_t smem_bytes(int n, int ring) { return 1024 + (size_t)ring * (a_stage_bytes() + b_stage_bytes(n)); }
 
 // one k-atom of A (128 rows from m0) and B (n rows) into a stage
 __device__ __forceinline__ void load_stage(const __nv_bfloat16* __restrict__ A, int lda, int m0,
@@ -57,14 +60,14 @@ __device__ __forceinline__ void load_stage(const __nv_bfloat16* __restrict__ A, 
     }
 }
 
-template <class Epi>
+template <int RING, class Epi>
 __global__ void __launch_bounds__(kThreads, 1) tcgemm_kernel(const __nv_bfloat16* __restrict__ A, int lda,
                                                              const __nv_bfloat16* __restrict__ B, int ldb,
                                                              int N, int kchunk, int K, Epi epi,
                                                              int* __restrict__ status)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bars[kRing + 1];
+    __shared__ __align__(8) uint64_t bars[RING + 1];
     __shared__ uint32_t tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int m0 = blockIdx.x * 128;
@@ -72,11 +75,11 @@ __global__ void __launch_bounds__(kThreads, 1) tcgemm_kernel(const __nv_bfloat16
     const int nk = (kend - kbeg) / 64;
     const uint32_t raw = tc::smem_addr(smem_raw);
     const uint32_t base = raw + ((1024u - (raw & 1023u)) & 1023u);
-    const uint32_t sa0 = base, sb0 = base + kRing * a_stage_bytes();
-    const uint32_t bar0 = tc::smem_addr(&bars[0]), done = tc::smem_addr(&bars[kRing]);
+    const uint32_t sa0 = base, sb0 = base + RING * a_stage_bytes();
+    const uint32_t bar0 = tc::smem_addr(&bars[0]), done = tc::smem_addr(&bars[RING]);
     const uint32_t ncols = N <= 32 ? 32u : N <= 64 ? 64u : N <= 128 ? 128u : 256u;
     if (tid == 0) {
-        for (int s = 0; s <= kRing; s++) tc::mbar_init(bar0 + 8 * s, 1);
+        for (int s = 0; s <= RING; s++) tc::mbar_init(bar0 + 8 * s, 1);
         tc::mbar_fence_init();
     }
     if (warp == 0) {
@@ -89,15 +92,15 @@ __global__ void __launch_bounds__(kThreads, 1) tcgemm_kernel(const __nv_bfloat16
     const uint32_t tmem = tmem_slot;
     const uint32_t idesc = tc::idesc_bf16_f32(128, N);
     bool ok = true;
-    // prologue: the first kRing - 1 atoms
-    for (int s = 0; s < kRing - 1; s++) {
+    // prologue: the first RING - 1 atoms
+    for (int s = 0; s < RING - 1; s++) {
         if (s < nk)
             load_stage(A, lda, m0, B, ldb, N, kbeg + 64 * s, sa0 + s * a_stage_bytes(), sb0 + s * b_stage_bytes(N));
         asm volatile("cp.async.commit_group;" ::: "memory");
     }
     for (int kc = 0; kc < nk; kc++) {
-        const int s = kc % kRing;
-        asm volatile("cp.async.wait_group %0;" ::"n"(kRing - 2) : "memory");
+        const int s = kc % RING;
+        asm volatile("cp.async.wait_group %0;" ::"n"(RING - 2) : "memory");
         tc::fence_async_smem();
         __syncthreads();
         if (tid == 0 && ok) {
@@ -108,15 +111,15 @@ __global__ void __launch_bounds__(kThreads, 1) tcgemm_kernel(const __nv_bfloat16
             for (int kk = 0; kk < 4; kk++) tc::mma_bf16(tmem, ad + 2 * kk, bd + 2 * kk, idesc, (kc | kk) != 0);
             tc::mma_commit(bar0 + 8 * s);
         }
-        const int nxt = kc + kRing - 1;
+        const int nxt = kc + RING - 1;
         if (nxt < nk) {
             if (kc >= 1) {  // the stage's previous atom (kc - 1) must have been consumed
-                const int sp = (kc - 1) % kRing;
-                if (!tc::mbar_wait(bar0 + 8 * sp, (uint32_t)((kc - 1) / kRing) & 1u, kWaitLimit)) ok = false;
+                const int sp = (kc - 1) % RING;
+                if (!tc::mbar_wait(bar0 + 8 * sp, (uint32_t)((kc - 1) / RING) & 1u, kWaitLimit)) ok = false;
             }
             if (ok)
-                load_stage(A, lda, m0, B, ldb, N, kbeg + 64 * nxt, sa0 + (nxt % kRing) * a_stage_bytes(),
-                           sb0 + (nxt % kRing) * b_stage_bytes(N));
+                load_stage(A, lda, m0, B, ldb, N, kbeg + 64 * nxt, sa0 + (nxt % RING) * a_stage_bytes(),
+                           sb0 + (nxt % RING) * b_stage_bytes(N));
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     }
@@ -149,6 +152,19 @@ __global__ void __launch_bounds__(kThreads, 1) tcgemm_kernel(const __nv_bfloat16
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
+template <int RING, class Epi>
+static cudaError_t launch_ring(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M, int N,
+                               int K, int kchunk, int splits, const Epi& epi, int* status, cudaStream_t s)
+{
+    const size_t smem = smem_bytes(N, RING);
+    cudaError_t e = cudaFuncSetAttribute(tcgemm_kernel<RING, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(M / 128, splits);
+    tcgemm_kernel<RING, Epi><<<grid, kThreads, smem, s>>>(A, lda, B, ldb, N, kchunk, K, epi, status);
+    return cudaGetLastError();
+}
+
 template <class Epi>
 static cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M, int N, int K,
                           int splits, const Epi& epi, int* status, cudaStream_t s)
@@ -156,13 +172,8 @@ static cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* 
     if (M % 128 || N % 16 || N < 16 || N > 256 || K % 64 || K < 64 || splits < 1) return cudaErrorInvalidValue;
     int kchunk = (K / 64 + splits - 1) / splits * 64;
     splits = (K + kchunk - 1) / kchunk;
-    const size_t smem = smem_bytes(N);
-    cudaError_t e = cudaFuncSetAttribute(tcgemm_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    dim3 grid(M / 128, splits);
-    tcgemm_kernel<Epi><<<grid, kThreads, smem, s>>>(A, lda, B, ldb, N, kchunk, K, epi, status);
-    return cudaGetLastError();
+    if (ring_for(kchunk / 64) == 2) return launch_ring<2>(A, lda, B, ldb, M, N, K, kchunk, splits, epi, status, s);
+    return launch_ring<4>(A, lda, B, ldb, M, N, K, kchunk, splits, epi, status, s);
 }
 
 // ---------------------------------------------------------------- epilogues

@@ -5,7 +5,7 @@
 
 namespace tp {
 namespace tct {
-size_t smem_bytes(int n);
+size_t smem_bytes(int n, int ring);
 }
 namespace tctrain {
 
