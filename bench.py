@@ -454,29 +454,73 @@ def secondary_modesum(tp, wl, args):
             "particles": na, "steps": sa,
             "spectrum_l1_surrogate_per_frame": l1_frames(rs["espect"], runs["fp64"]["espect"]),
             "diffusion_rel_err_surrogate": diffusion_errors(rs["dsum"], runs["fp64"]["dsum"])}
+        c4["gain_4096_modes"] = surrogate_gain(tp, wl, cfg, args, dom)
     except Exception as e:  # the C3 figures stand without it
         c4["error"] = str(e)
     return c3, c4
 
 
-def train_surrogate(tp, modes, cfg, args):
-    """Train the learned field on samples of the exact mode sum and measure
-    its field error on fresh points."""
-    amp = np.linalg.norm(modes["amp_b"], axis=1)
-    freq = modes["n"][np.argsort(-amp)[:64]]
-    tp.mlp_init(freq, seed=3)
-    loss, ms = tp.mlp_train(16777216, 65536, args.epochs, lr=2e-3)
+def field_errors(tp, B0, model=None, exact=None):
+    """Relative RMS errors of dB and E against the current (exact) field on
+    65,536 fixed points; model None: the tensor-core model's field."""
     rng = np.random.default_rng(5)
     u = rng.integers(0, 2 ** 32, size=(65536, 3), dtype=np.uint64).astype(np.uint32)
     xyzt = np.zeros((len(u), 4))
     xyzt[:, :3] = u / 2 ** 32
-    exact = tp.get_emf(xyzt)
-    model = tp.mlp_eval_kernel(u)
-    dB = exact[:, :3] - [0, 0, cfg["B0"]]
-    return {"samples": 16777216, "epochs": args.epochs, "final_loss": loss, "train_ms": ms,
-            "rel_rms_err_dB": float(np.sqrt(np.mean((model[:, :3] - exact[:, :3]) ** 2) / np.mean(dB ** 2))),
-            "rel_rms_err_E": float(np.sqrt(np.mean((model[:, 3:] - exact[:, 3:]) ** 2) /
-                                           np.mean(exact[:, 3:] ** 2)))}
+    ex = tp.get_emf(xyzt) if exact is None else exact
+    md = tp.mlp_eval_kernel(u) if model is None else model
+    dB = ex[:, :3] - [0, 0, B0]
+    return (float(np.sqrt(np.mean((md[:, :3] - ex[:, :3]) ** 2) / np.mean(dB ** 2))),
+            float(np.sqrt(np.mean((md[:, 3:] - ex[:, 3:]) ** 2) / np.mean(ex[:, 3:] ** 2))), ex, xyzt)
+
+
+def train_surrogate(tp, modes, cfg, args, samples=16777216):
+    """Train the learned field on samples of the exact mode sum (features: the
+    64 strongest distinct lattice vectors) and measure its field error on
+    fresh points."""
+    import test_particle_gb300.workloads as wl
+    tp.mlp_init(wl.surrogate_features(modes), seed=3)
+    loss, ms = tp.mlp_train(samples, 65536, args.epochs, lr=2e-3)
+    eb, ee, _, _ = field_errors(tp, cfg["B0"])
+    flop = 3 * 2 * (128 * 256 + 3 * 256 * 256 + 256 * 6) * samples * args.epochs
+    return {"samples": samples, "epochs": args.epochs, "final_loss": loss, "train_ms": ms,
+            "train_tflops": flop / (ms * 1e-3) / 1e12, "rel_rms_err_dB": eb, "rel_rms_err_E": ee}
+
+
+def surrogate_gain(tp, wl, cfg, args, dom, nmodes=4096):
+    """What the trained model gains over the method without it, on a field of
+    nmodes modes with the same spectrum: pushes/s of the model against the
+    exact FP32 sum, and, at equal cost, its field error against the exact sum
+    truncated to the K strongest modes that run at the model's speed."""
+    big = wl.kolmogorov_modes(nmodes, cfg["kmin"], cfg["kmax"], cfg["dB"], cfg["seed"] + 5, va=cfg["va"])
+    tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=big, mode_B0=cfg["B0"])
+    tp.set_spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
+    train = train_surrogate(tp, big, cfg, args)
+    dt = cfg["dt"]
+    tp.set_tmax(50 * dt + 0.5 * dt)
+    p0 = wl.shell_particles(1048576, cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"] + 6)
+    s = tp.Session(len(p0))
+    r = {}
+    try:
+        for label, code in (("exact_fp32_sum", tp.PREC_MIXED), ("model", tp.PREC_SURROGATE)):
+            best = None
+            for _ in range(2):
+                s.load(p0)
+                info = s.track(dt, 1, cfg["nbins"], code)
+                best = info.kernel_ms if best is None else min(best, info.kernel_ms)
+            r[label] = info.pushes / best * 1e3
+    finally:
+        s.close()
+    keq = max(1, int(nmodes * r["exact_fp32_sum"] / r["model"]))
+    # the exact sum truncated to the keq strongest modes, measured on the same points
+    _, _, exact, xyzt = field_errors(tp, cfg["B0"], model=np.zeros((65536, 6)))
+    top = big[np.argsort(-np.linalg.norm(big["amp_b"], axis=1))[:keq]]
+    tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=top, mode_B0=cfg["B0"])
+    eb_t, ee_t, _, _ = field_errors(tp, cfg["B0"], model=tp.get_emf(xyzt), exact=exact)
+    return {"modes": nmodes, "train": train, "pushes_per_s": r,
+            "model_over_exact_sum": r["model"] / r["exact_fp32_sum"],
+            "equal_cost_modes": keq, "truncated_sum_rel_rms_err_dB": eb_t, "truncated_sum_rel_rms_err_E": ee_t,
+            "model_more_accurate_at_equal_cost": bool(train["rel_rms_err_dB"] < eb_t)}
 
 
 def bs_setup(tp):
@@ -831,7 +875,7 @@ def main():
                     help="one workload on its own instead of the headline line")
     ap.add_argument("--nptl", type=int, default=0)
     ap.add_argument("--run-steps", type=int, default=0)
-    ap.add_argument("--epochs", type=int, default=4)
+    ap.add_argument("--epochs", type=int, default=16)
     ap.add_argument("--cpu-bs", action="store_true")
     ap.add_argument("--profile", choices=["mixed", "mixed512", "fp64", "fp64fast", "surrogate", "modesum",
                                           "abc"],

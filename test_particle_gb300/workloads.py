@@ -48,6 +48,28 @@ def kolmogorov_modes(nmodes, nmin, nmax, rms, seed, va=0.0, index=-5.0 / 3.0):
     return out
 
 
+def surrogate_features(modes, k=64):
+    """Fourier-feature frequencies of the learned field: the k strongest
+    distinct lattice vectors of a mode table, up to sign, by the energy of the
+    plane waves that share each vector (modes whose n round to the same lattice
+    vector add to one plane wave, sum_m a_m exp(+-i phase_m)).  Low-|n| vectors
+    recur among many modes, so taking the k strongest *modes* instead would
+    repeat a few vectors and leave features unused."""
+    acc = {}
+    for q in np.asarray(modes):
+        n = tuple(int(v) for v in q["n"])
+        m = tuple(-v for v in n)
+        c, sgn = (n, 1.0) if n >= m else (m, -1.0)
+        acc[c] = acc.get(c, 0) + q["amp_b"] * np.exp(1j * sgn * q["phase"])
+    order = sorted(acc, key=lambda c: (-float(np.sum(np.abs(acc[c]) ** 2)), c))
+    out = np.zeros((k, 3), dtype=np.int32)
+    for i, c in enumerate(order[:k]):
+        out[i] = c
+    for i in range(len(order), k):  # fewer distinct vectors than features: unit axes
+        out[i] = [(i % 3) == 0, (i % 3) == 1, (i % 3) == 2]
+    return out
+
+
 def shell_particles(n, speed, lo, hi, seed, qm=1.0):
     """Uniform positions in [lo, hi), isotropic momenta with |v| = speed (c = 1)."""
     rng = np.random.default_rng(seed)

@@ -85,6 +85,10 @@ def test_training_learns_a_small_field():
 
 
 def test_surrogate_tracking_runs_and_tracks_the_exact_field():
+    """Tracking with the trained model of a 16-mode field against tracking
+    with the exact FP32 sum: per output frame the spectra differ by no more
+    than two independent ensembles of this size drawn from the exact run's
+    spectrum would (the sampling floor) plus 3 sigma of that distance."""
     modes = small_modes()
     dom = tp.Domain()
     dom.xmax = dom.ymax = dom.zmax = 1.0
@@ -98,13 +102,18 @@ def test_surrogate_tracking_runs_and_tracks_the_exact_field():
     tp.mlp_init(freq, seed=9)
     tp.mlp_train(1 << 20, 8192, 3, lr=2e-3)
     tp.set_spectrum(200, 1e-3, 1e2)
-    p0 = wl.shell_particles(4096, 0.7, (0, 0, 0), (1, 1, 1), 8)
+    n = 16384
+    p0 = wl.shell_particles(n, 0.7, (0, 0, 0), (1, 1, 1), 8)
     a = tp.track(p0, dt, 4, 200, precision=tp.PREC_MIXED)
     b = tp.track(p0, dt, 4, 200, precision=tp.PREC_SURROGATE)
-    assert b["espect"].sum() == a["espect"].sum() == 4 * 4096
+    assert b["espect"].sum() == a["espect"].sum() == 4 * n
     assert np.all(b["nsteps"] == steps + 1)
-    sa, sb = a["espect"] / 4096, b["espect"] / 4096
-    assert np.all(np.abs(sa - sb).sum(axis=1) < 0.5)
+    l1 = np.abs(a["espect"] / n - b["espect"] / n).sum(axis=1)
+    q = a["espect"] / n
+    floor = np.sqrt(4 * q * (1 - q) / (np.pi * n)).sum(axis=1)
+    sigma = np.sqrt(2 * (1 - 2 / np.pi) / n)
+    print("surrogate vs exact L1 %s sampling floor %s" % (l1, floor))
+    assert np.all(l1 <= floor + 3 * sigma), (l1, floor)
     assert tp.device_status() == 0
 
 
@@ -169,12 +178,15 @@ def test_tensor_core_inference_matches_fp64_forward():
     assert tp.device_status() == 0
 
 
-def test_model_cost_does_not_grow_with_the_mode_count():
-    """What the learned field gains over the method without it: the exact
-    plane-wave sum costs in proportion to its modes, the model a fixed chain
-    of GEMMs; at 4096 modes tracking with the model is faster than with the
-    exact FP32 sum (an untrained model does the same work as a trained one)."""
-    modes = wl.kolmogorov_modes(4096, 1, 64, 1.0, 5, va=0.1)
+def test_trained_model_gains_over_the_exact_sum():
+    """What the trained model gains over the method without it, on a field of
+    4096 plane waves with the workload's spectrum: tracking with the model is
+    more than 3x faster than with the exact FP32 sum (its cost does not grow
+    with the mode count), and at equal cost -- the exact sum truncated to the
+    K strongest modes that run as fast as the model -- its field error is the
+    smaller one."""
+    cfg = wl.config_modesum()
+    modes = wl.kolmogorov_modes(4096, cfg["kmin"], cfg["kmax"], cfg["dB"], cfg["seed"] + 5, va=cfg["va"])
     dom = tp.Domain()
     dom.xmax = dom.ymax = dom.zmax = 1.0
     steps = 20
@@ -182,19 +194,32 @@ def test_model_cost_does_not_grow_with_the_mode_count():
     dom.tmax = steps * dt + 0.5 * dt
     tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=1.0)
     tp.set_spectrum(200, 1e-3, 1e2)
-    amp = np.linalg.norm(modes["amp_b"], axis=1)
-    tp.mlp_init(modes["n"][np.argsort(-amp)[:64]], seed=3)
-    tp.mlp_set_output_norm(np.array([0, 0, 1, 0, 0, 0]), np.ones(6))
-    p0 = wl.shell_particles(65536, 0.7, (0, 0, 0), (1, 1, 1), 6)
+    tp.mlp_init(wl.surrogate_features(modes), seed=3)
+    tp.mlp_train(1 << 24, 65536, 16, lr=2e-3)
+    rng = np.random.default_rng(2)
+    u = rng.integers(0, 2 ** 32, size=(65536, 3), dtype=np.uint64).astype(np.uint32)
+    xyzt = np.zeros((len(u), 4))
+    xyzt[:, :3] = u / 2 ** 32
+    exact = tp.get_emf(xyzt)
+    db2 = np.mean((exact[:, :3] - [0, 0, 1]) ** 2)
+    err_model = np.sqrt(np.mean((tp.mlp_eval_kernel(u)[:, :3] - exact[:, :3]) ** 2) / db2)
+    p0 = wl.shell_particles(262144, 0.7, (0, 0, 0), (1, 1, 1), 6)
     s = tp.Session(len(p0))
-    ms = {}
+    rate = {}
     for label, code in (("exact", tp.PREC_MIXED), ("model", tp.PREC_SURROGATE)):
         best = None
         for _ in range(2):  # the first run includes one-time set-up
             s.load(p0)
             info = s.track(dt, 1, 200, code)
             best = info.kernel_ms if best is None else min(best, info.kernel_ms)
-        ms[label] = best
+        rate[label] = info.pushes / best
     s.close()
-    assert ms["exact"] > 1.3 * ms["model"], ms
+    k = int(4096 * rate["exact"] / rate["model"])
+    top = modes[np.argsort(-np.linalg.norm(modes["amp_b"], axis=1))[:k]]
+    tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=top, mode_B0=1.0)
+    err_trunc = np.sqrt(np.mean((tp.get_emf(xyzt)[:, :3] - exact[:, :3]) ** 2) / db2)
+    print("model %.3gx the exact sum's pushes/s; field error model %.3f, exact sum of the %d strongest "
+          "modes %.3f" % (rate["model"] / rate["exact"], err_model, k, err_trunc))
+    assert rate["model"] > 3 * rate["exact"], rate
+    assert err_model < err_trunc, (err_model, err_trunc, k)
     assert tp.device_status() == 0
