@@ -744,6 +744,22 @@ def profile_case(prec):
     for abc."""
     import test_particle_gb300 as tp
     import test_particle_gb300.workloads as wl
+    if prec == "train":
+        # one epoch of the learned field's training on 1,048,576 samples of the
+        # 512-mode field, batch 65,536 (16 steps)
+        tp.check(tp.lib().tp_init(0), "tp_init")
+        cfg = wl.config_modesum()
+        dom = tp.Domain()
+        dom.xmax = dom.ymax = dom.zmax = 1.0
+        modes = wl.kolmogorov_modes(cfg["nmodes"], cfg["kmin"], cfg["kmax"], cfg["dB"], cfg["seed"],
+                                    va=cfg["va"])
+        tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=cfg["B0"])
+        tp.mlp_init(wl.surrogate_features(modes), seed=3)
+        loss, ms = tp.mlp_train(1 << 20, 65536, 1, lr=2e-3)
+        flop = 3 * 2 * (128 * 256 + 3 * 256 * 256 + 256 * 6) * (1 << 20)
+        print(json.dumps({"profile": "train", "train_ms": ms, "ms_per_batch": ms / 16,
+                          "train_tflops": flop / (ms * 1e-3) / 1e12}))
+        return
     if prec == "abc":
         tp.check(tp.lib().tp_init(0), "tp_init")
         cfg = wl.config_abc(steps=1000)
@@ -765,8 +781,7 @@ def profile_case(prec):
         tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=cfg["B0"])
         tp.set_spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
         if prec == "surrogate":
-            amp = np.linalg.norm(modes["amp_b"], axis=1)
-            tp.mlp_init(modes["n"][np.argsort(-amp)[:64]], seed=3)
+            tp.mlp_init(wl.surrogate_features(modes), seed=3)
             tp.mlp_set_output_norm(np.array([0, 0, 1, 0, 0, 0]), np.ones(6))
         p0 = wl.shell_particles(cfg["nptl"], cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"])
     elif prec == "mixed512":
@@ -878,12 +893,13 @@ def main():
     ap.add_argument("--epochs", type=int, default=16)
     ap.add_argument("--cpu-bs", action="store_true")
     ap.add_argument("--profile", choices=["mixed", "mixed512", "fp64", "fp64fast", "surrogate", "modesum",
-                                          "abc"],
+                                          "abc", "train"],
                     default=None,
                     help="one tracking launch of a small case for a profiler capture (gridded "
                          "field 256^3, 131072 particles, 200 steps; mixed512: the 512^3 headline field "
                          "and particles, 200 steps; surrogate and modesum: 512-mode field, 155648 "
-                         "particles, 20 steps; abc: 65536 particles, 1000 steps)")
+                         "particles, 20 steps; abc: 65536 particles, 1000 steps; train: one training "
+                         "epoch of the learned field on 1,048,576 samples)")
     args = ap.parse_args()
     if args.profile:
         profile_case(args.profile)

@@ -48,6 +48,47 @@ enum : int { DG_SG = 0, DG_X0 = 8, DG_U0 = 11, DG_T0 = 14, DG_MU0 = 15, DG_G0 = 
 #ifndef TP_MIXED_PIC_MINBLOCKS
 #define TP_MIXED_PIC_MINBLOCKS 4
 #endif
+#ifndef TP_MIXED_PREFETCH
+#define TP_MIXED_PREFETCH 0
+#endif
+
+// The diffusion singles of one particle at a diffusion step
+// (calc_diff_coeff, src/diagnostics.c:659-705), FP64 accumulation, into its
+// rows of dg; one FP64 reciprocal of 2t + dt instead of eight divisions (the
+// FP64 pipe runs at a small fraction of the FP32 rate).  The pitch angle
+// needs the field at the particle, evaluated with the particle's cell cache.
+// (Compiled as a separate function, with a cache of its own, this costs the
+// step loop spills at its call site instead of saving registers: measured
+// by -Xptxas -v, 24-32 B at 4 blocks per SM, 132-152 B at 5.)
+template <int SYS>
+__device__ __forceinline__ void diff_singles_body(const MixField& f, const PM& p, const ModePair* smodes,
+                                                  FieldCache& fc, double (*dg)[kBlock], int tx, int done, double qdt)
+{
+    double t = dg[DG_T0][tx] + done * qdt;
+    double itt = 1.0 / (t * 2 + qdt);
+    double dd[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        double pos = (double)p.X[k] * 5.421010862427522e-20 + p.img[k];
+        dd[k] = dg[DG_X0 + k][tx] - (f.min[k] + f.L[k] * pos);
+    }
+    const double u00 = dg[DG_U0][tx], u01 = dg[DG_U0 + 1][tx], u02 = dg[DG_U0 + 2][tx];
+    const double mu0 = dg[DG_MU0][tx];
+    double dxx = dd[0] * dd[0] * itt, dyy = dd[1] * dd[1] * itt, dzz = dd[2] * dd[2] * itt;
+    double du0 = u00 - p.u[0], du1 = u01 - p.u[1], du2 = u02 - p.u[2];
+    double g1 = sqrt(1.0 + (double)p.u[0] * p.u[0] + (double)p.u[1] * p.u[1] + (double)p.u[2] * p.u[2]);
+    double g0 = dg[DG_G0][tx];
+    double mu = pitch_mu<SYS>(f, p.X, p.u, smodes, fc);
+    double th = (double)acosf((float)mu) * (180.0 / 3.14159265358979323846);
+    double th0 = (double)acosf((float)mu0) * (180.0 / 3.14159265358979323846);
+    dg[DG_SG + 1][tx] = dxx; dg[DG_SG + 2][tx] = dyy; dg[DG_SG + 3][tx] = dzz;
+    dg[DG_SG + 0][tx] = dxx + dyy + dzz;
+    dg[DG_SG + 4][tx] = (du0 * du0 + du1 * du1 + du2 * du2) * itt;
+    dg[DG_SG + 5][tx] = (mu - mu0) * (mu - mu0) * itt;
+    dg[DG_SG + 6][tx] = (th - th0) * (th - th0) * itt;
+    dg[DG_SG + 7][tx] = (g1 - g0) * (g1 - g0) * itt;
+}
+
 
 // Persistent fixed-step tracking in mixed precision: the same schedule and
 // diagnostics as the FP64 kernel (src/tracking.c:297-462); the mode table of
@@ -138,39 +179,16 @@ __global__ void __launch_bounds__(kBlock, SYS == TP_SYS_PIC ? TP_MIXED_PIC_MINBL
             to_frame = at_frame ? q.einterval - 1 : to_frame - 1;
             if (active && (esc_pre == 0 || f.bc_flag == 0)) {
                 bool e2 = false;
+                float step[3];
                 wirz_f32(f, p, dt, [&](const uint64_t* X, float* E, float* B) {
                     field_mixed<SYS>(f, X, E, B, smodes, fc);
-                }, e2);
+                }, e2, step);
+                if (SYS == TP_SYS_PIC && TP_MIXED_PREFETCH) prefetch_next_cell(f, p.X, step);
                 if (e2) esc_after = 1;
                 nst += 1;
                 done += 1;
                 if (esc_after == 0 && at_diff) {
-                    // calc_diff_coeff, src/diagnostics.c:659-705, FP64 accumulation;
-                    // one FP64 reciprocal of 2t + dt instead of eight divisions
-                    // (the FP64 pipe runs at a small fraction of the FP32 rate)
-                    double t = dg[DG_T0][tx] + done * q.dt;
-                    double itt = 1.0 / (t * 2 + q.dt);
-                    double dd[3];
-#pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                        double pos = (double)p.X[k] * 5.421010862427522e-20 + p.img[k];
-                        dd[k] = dg[DG_X0 + k][tx] - (f.min[k] + f.L[k] * pos);
-                    }
-                    const double u00 = dg[DG_U0][tx], u01 = dg[DG_U0 + 1][tx], u02 = dg[DG_U0 + 2][tx];
-                    const double mu0 = dg[DG_MU0][tx];
-                    double dxx = dd[0] * dd[0] * itt, dyy = dd[1] * dd[1] * itt, dzz = dd[2] * dd[2] * itt;
-                    double du0 = u00 - p.u[0], du1 = u01 - p.u[1], du2 = u02 - p.u[2];
-                    double g1 = sqrt(1.0 + (double)p.u[0] * p.u[0] + (double)p.u[1] * p.u[1] + (double)p.u[2] * p.u[2]);
-                    double g0 = dg[DG_G0][tx];
-                    double mu = pitch_mu<SYS>(f, p.X, p.u, smodes, fc);
-                    double th = (double)acosf((float)mu) * (180.0 / 3.14159265358979323846);
-                    double th0 = (double)acosf((float)mu0) * (180.0 / 3.14159265358979323846);
-                    dg[DG_SG + 1][tx] = dxx; dg[DG_SG + 2][tx] = dyy; dg[DG_SG + 3][tx] = dzz;
-                    dg[DG_SG + 0][tx] = dxx + dyy + dzz;
-                    dg[DG_SG + 4][tx] = (du0 * du0 + du1 * du1 + du2 * du2) * itt;
-                    dg[DG_SG + 5][tx] = (mu - mu0) * (mu - mu0) * itt;
-                    dg[DG_SG + 6][tx] = (th - th0) * (th - th0) * itt;
-                    dg[DG_SG + 7][tx] = (g1 - g0) * (g1 - g0) * itt;
+                    diff_singles_body<SYS>(f, p, smodes, fc, dg, tx, done, q.dt);
                 }
             }
             if (active && esc_pre == 0 && esc_after == 1 && f.bc_flag == 1 && ntp < q.nt_out)
