@@ -125,33 +125,6 @@ __device__ __forceinline__ uint32_t cell_and_weights(const MixField& f, const ui
     return (uint32_t)ix + (uint32_t)f.nx * iy + (uint32_t)f.nx * f.ny * iz;
 }
 
-// Asks L1 for the eight corner nodes of the cell that the position X + step
-// (step in box fractions, the displacement of the step just taken) lies in,
-// when that is not X's own cell: the cell the particle is expected to reach
-// one step later.  A prefetch changes no value; a wrong guess costs cache
-// space only.
-__device__ __forceinline__ void prefetch_next_cell(const MixField& f, const uint64_t X[3], const float step[3])
-{
-    uint32_t key[2];
-    int ic[2][3];
-#pragma unroll
-    for (int w = 0; w < 2; w++) {
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const uint32_t x32 = (uint32_t)(X[k] >> 32) + (w ? (uint32_t)__float2int_rn(step[k] * 4294967296.0f) : 0u);
-            const int n = k == 0 ? f.nx : k == 1 ? f.ny : f.nz;
-            ic[w][k] = (int)(((uint64_t)x32 * (uint32_t)(n - 1)) >> 32);
-        }
-        key[w] = (uint32_t)ic[w][0] + (uint32_t)f.nx * ic[w][1] + (uint32_t)f.nx * f.ny * ic[w][2];
-    }
-    if (key[1] == key[0]) return;
-    const uint32_t nx = f.nx, nxy = (uint32_t)f.nx * f.ny;
-    const float4* p = f.eb + (size_t)key[1] * 2;
-    const uint32_t off[8] = {0, 1, nx, nx + 1, nxy, nxy + 1, nxy + nx, nxy + nx + 1};
-#pragma unroll
-    for (int c = 0; c < 8; c++) asm volatile("prefetch.global.L1 [%0];" ::"l"(p + (size_t)off[c] * 2));
-}
-
 // Trilinear E and B from the node-interleaved grid: the eight corner weights
 // once, then per pair of components one multiply and seven packed FMAs, in
 // corner order (each component's products and sums are those of a scalar

@@ -48,9 +48,7 @@ enum : int { DG_SG = 0, DG_X0 = 8, DG_U0 = 11, DG_T0 = 14, DG_MU0 = 15, DG_G0 = 
 #ifndef TP_MIXED_PIC_MINBLOCKS
 #define TP_MIXED_PIC_MINBLOCKS 4
 #endif
-#ifndef TP_MIXED_PREFETCH
-#define TP_MIXED_PREFETCH 0
-#endif
+
 
 // The diffusion singles of one particle at a diffusion step
 // (calc_diff_coeff, src/diagnostics.c:659-705), FP64 accumulation, into its
@@ -179,11 +177,9 @@ __global__ void __launch_bounds__(kBlock, SYS == TP_SYS_PIC ? TP_MIXED_PIC_MINBL
             to_frame = at_frame ? q.einterval - 1 : to_frame - 1;
             if (active && (esc_pre == 0 || f.bc_flag == 0)) {
                 bool e2 = false;
-                float step[3];
                 wirz_f32(f, p, dt, [&](const uint64_t* X, float* E, float* B) {
                     field_mixed<SYS>(f, X, E, B, smodes, fc);
-                }, e2, step);
-                if (SYS == TP_SYS_PIC && TP_MIXED_PREFETCH) prefetch_next_cell(f, p.X, step);
+                }, e2);
                 if (e2) esc_after = 1;
                 nst += 1;
                 done += 1;

@@ -43,10 +43,9 @@ __device__ __forceinline__ void advance(uint64_t& X, int& img, float fr)
 }
 
 // One Wirz push; field(X, E, B) evaluates the field at a fixed-point position.
-// With step_out the step's displacement (box fractions per axis) is returned.
 template <class FieldFn>
 __device__ __forceinline__ void wirz_f32(const MixField& f, PM& p, float dt, FieldFn&& field,
-                                         bool& escaped, float* step_out = nullptr)
+                                         bool& escaped)
 {
     // Norms and their inverses come from one rsqrt each (a single SFU
     // operation, a few ulp): the FP32 path's error budget is set by FP32
@@ -114,7 +113,6 @@ __device__ __forceinline__ void wirz_f32(const MixField& f, PM& p, float dt, Fie
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         float d = (h[k] * a1 + hp[k] * a2 + hr[k] * a3) * f.invL[k];
-        if (step_out) step_out[k] = d;
         if (f.bc_flag == 1) {
             // open boundary: leaving the box is an escape, not a wrap
             int before = p.img[k];
