@@ -8,7 +8,9 @@
 #pragma once
 #include "tp_common.cuh"
 
-#define TP_ELL_QUAL __constant__ static const
+// In global memory, read through L1: the lanes of a warp index different
+// intervals, and constant-cache reads of different addresses serialise.
+#define TP_ELL_QUAL __device__ static const
 #include "ellint_coeffs.h"
 #undef TP_ELL_QUAL
 
@@ -202,13 +204,17 @@ __device__ __forceinline__ void ellint64(double k, int corrected, double& elle, 
     else if (m >= 0.85 && m < 0.9) i = 9;
     else i = 10;
     if (i >= 0 && i <= 9) {
-        double m1 = m - tp_ell_m0[i], powj = 1.0;
-        int nk = tp_ell_nk[i], ne = tp_ell_ne[i];
-        for (int j = 0; j < nk; j++) {
-            double kc = tp_ell_k[i][j];
+        // every lane runs the longest series of the table: past an interval's
+        // own length its coefficients are zero and add +0 exactly, so the
+        // sums are those of the interval's own length while the lanes of a
+        // warp, whatever their intervals, take the same loop
+        double m1 = m - __ldg(&tp_ell_m0[i]), powj = 1.0;
+#pragma unroll
+        for (int j = 0; j < TP_ELL_NK_MAX; j++) {
+            double kc = __ldg(&tp_ell_k[i][j]);
             if (!corrected && i == 9 && j == 19) kc = TP_ELL_K9_19_REF;
             ellf += kc * powj;
-            if (j < ne) elle += tp_ell_e[i][j] * powj;
+            if (j < TP_ELL_NE_MAX) elle += __ldg(&tp_ell_e[i][j]) * powj;
             powj *= m1;
         }
         return;
@@ -216,19 +222,19 @@ __device__ __forceinline__ void ellint64(double k, int corrected, double& elle, 
     double ellf1 = 0.0, q1 = 0.0, hm = 0.0, powj = 1.0;
     double m1 = corrected ? (0.95 - m) : (m - 0.95);
     for (int j = 0; j <= 10; j++) {
-        ellf1 += tp_ell_k[0][j] * powj;
+        ellf1 += __ldg(&tp_ell_k[0][j]) * powj;
         powj *= m1;
     }
     m1 = 1.0 - m;
     powj = m1;
     for (int j = 1; j <= 14; j++) {
-        q1 += tp_ell_q[j] * powj;
+        q1 += __ldg(&tp_ell_q[j]) * powj;
         powj *= m1;
     }
     powj = 1.0;
     m1 = 0.95 - m;
     for (int j = 0; j <= 10; j++) {
-        hm += tp_ell_h[j] * powj;
+        hm += __ldg(&tp_ell_h[j]) * powj;
         powj *= m1;
     }
     ellf = -log(q1) * (ellf1 / TP_PI);
