@@ -35,7 +35,10 @@ constexpr uint32_t kWaitLimit = 1u << 22;
 
 __host__ __device__ constexpr uint32_t a_stage_bytes() { return 128u * 128u; }
 __host__ __device__ constexpr uint32_t b_stage_bytes(int n) { return (uint32_t)n * 128u; }
-__host__ __device__ constexpr int ring_for(int k_atoms) { return k_atoms <= 4 ? 2 : 4; }
+#ifndef TP_TCT_SHORT_RING
+#define TP_TCT_SHORT_RING 2
+#endif
+__host__ __device__ constexpr int ring_for(int k_atoms) { return k_atoms <= 4 ? TP_TCT_SHORT_RING : 4; }
 size_t smem_bytes(int n, int ring) { return 1024 + (size_t)ring * (a_stage_bytes() + b_stage_bytes(n)); }
 
 // one k-atom of A (128 rows from m0) and B (n rows) into a stage
@@ -126,6 +129,10 @@ __global__ void __launch_bounds__(kThreads, 1) tcgemm_kernel(const __nv_bfloat16
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     ok = __syncthreads_and(ok) != 0;
     if (tid == 0) tc::mma_commit(done);
+    // operands of the epilogue that do not depend on the MMAs (the SiLU
+    // derivative's pre-activations) are loaded while they finish
+    Epi e = epi;
+    if (ok && nk > 0) e.begin(m0 + tid);
     const bool fine = tc::mbar_wait(done, 0, kWaitLimit);
     if (!(ok && fine) && (tid & 31) == 0) atomicOr(status, ST_TIMEOUT);
     tc::tc_fence_after();
@@ -133,18 +140,22 @@ __global__ void __launch_bounds__(kThreads, 1) tcgemm_kernel(const __nv_bfloat16
         const int row = m0 + tid;
         const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
         if (N >= 32) {
-            // 32 columns at a time; a last chunk of 16 (N an odd multiple of
-            // 16) reads 16 columns past N inside the allocation and hands on
-            // only the 16 that exist
-            for (int c = 0; c < N; c += 32) {
-                float v[32];
-                tc::tmem_ld32(tmem + lane_base + (uint32_t)c, v);
-                epi(row, c, v, min(32, N - c));
+            // 32 columns at a time (unrolled, so that per-row values an
+            // epilogue holds stay in registers); a last chunk of 16 (N an odd
+            // multiple of 16) reads 16 columns past N inside the allocation
+            // and hands on only the 16 that exist
+#pragma unroll
+            for (int c = 0; c < 256; c += 32) {
+                if (c < N) {
+                    float v[32];
+                    tc::tmem_ld32(tmem + lane_base + (uint32_t)c, v);
+                    e(row, c, v, min(32, N - c));
+                }
             }
         } else {
             float v[32];
             tc::tmem_ld16(tmem + lane_base, v);
-            epi(row, 0, v, 16);
+            e(row, 0, v, 16);
         }
     }
     tc::tc_fence_before();
@@ -181,6 +192,7 @@ static cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* 
 struct EpiStoreF32 {  // D[m][n] = acc (self-check)
     float* D;
     int ld;
+    __device__ void begin(int) {}
     __device__ void operator()(int m, int c0, const float* v, int cnt) const
     {
         for (int i = 0; i < cnt; i++) D[(size_t)m * ld + c0 + i] = v[i];
@@ -192,6 +204,7 @@ struct EpiHiddenT {
     const float* b;
     __nv_bfloat16 *Z, *H, *HT;
     int M;
+    __device__ void begin(int) {}
     __device__ void operator()(int m, int c0, const float* v, int cnt) const
     {
 #pragma unroll
@@ -219,22 +232,31 @@ struct EpiHiddenT {
 struct EpiOutT {
     const float* b;
     float* Y;
+    __device__ void begin(int) {}
     __device__ void operator()(int m, int c0, const float* v, int cnt) const
     {
         for (int c = 0; c < mlp::kOut; c++) Y[(size_t)m * mlp::kOut + c] = v[c] + b[c];
     }
 };
 
-// g = acc * silu'(Z): G row-major [M][256] and transposed [256][M]
+// g = acc * silu'(Z): G row-major [M][256] and transposed [256][M]; the row's
+// 256 pre-activations are loaded in one burst (begin) while the MMAs finish
 struct EpiBackSiluT {
     const __nv_bfloat16* Z;
     __nv_bfloat16 *G, *GT;
     int M;
+    uint4 zrow[mlp::kHid / 8];
+    __device__ void begin(int m)
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(Z + (size_t)m * mlp::kHid);
+#pragma unroll
+        for (int i = 0; i < mlp::kHid / 8; i++) zrow[i] = __ldg(src + i);
+    }
     __device__ void operator()(int m, int c0, const float* v, int cnt) const
     {
 #pragma unroll
         for (int i = 0; i < 32; i += 8) {
-            const uint4 zr = *reinterpret_cast<const uint4*>(Z + (size_t)m * mlp::kHid + c0 + i);
+            const uint4 zr = zrow[(c0 + i) / 8];
             const uint32_t zw[4] = {zr.x, zr.y, zr.z, zr.w};
             uint32_t gp[4];
 #pragma unroll
@@ -259,6 +281,7 @@ struct EpiBackSiluT {
 struct EpiPartial {
     float* P;
     int M, N;
+    __device__ void begin(int) {}
     __device__ void operator()(int m, int c0, const float* v, int cnt) const
     {
         float* dst = P + ((size_t)blockIdx.y * M + m) * N + c0;
