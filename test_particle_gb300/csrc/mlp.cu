@@ -26,21 +26,11 @@ namespace tp {
 namespace mlp {
 
 // ---------------------------------------------------------------- features
-// X[b][j] = sin(2 pi f_j . u_b), X[b][64 + j] = cos(...); u as 32-bit fixed point
-__device__ __forceinline__ void features_row(const int* freq, uint32_t U0, uint32_t U1, uint32_t U2,
-                                             __nv_bfloat16* xrow)
-{
-    for (int j = 0; j < kFeat; j++) {
-        uint32_t ph = (uint32_t)freq[3 * j] * U0 + (uint32_t)freq[3 * j + 1] * U1 +
-                      (uint32_t)freq[3 * j + 2] * U2;
-        float s, c;
-        __sincosf(mixed::rev_to_rad(ph), &s, &c);
-        xrow[j] = __float2bfloat16(s);
-        xrow[kFeat + j] = __float2bfloat16(c);
-    }
-}
-
-// X [n][128]; with XT, also transposed [128][n] (the weight-gradient operand)
+// X[b][j] = sin(2 pi f_j . u_b), X[b][64 + j] = cos(...) with u in 32-bit fixed
+// point, as BF16 [n][128]; with XT, also transposed [128][n] (the
+// weight-gradient operand).  Eight features at a time: the row is written in
+// 16-byte pieces, the transposed copy one column at a time (a warp writes 32
+// consecutive samples of a column).
 __global__ void features_kernel(const uint32_t* __restrict__ U, int n, const int* __restrict__ freq,
                                 __nv_bfloat16* __restrict__ X, __nv_bfloat16* __restrict__ XT = nullptr)
 {
@@ -49,10 +39,34 @@ __global__ void features_kernel(const uint32_t* __restrict__ U, int n, const int
     __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    __nv_bfloat16* row = X + (size_t)i * kIn;
-    features_row(fs, U[3 * i], U[3 * i + 1], U[3 * i + 2], row);
-    if (XT)
-        for (int j = 0; j < kIn; j++) XT[(size_t)j * n + i] = row[j];
+    const uint32_t U0 = U[3 * i], U1 = U[3 * i + 1], U2 = U[3 * i + 2];
+    uint4* row = reinterpret_cast<uint4*>(X + (size_t)i * kIn);
+#pragma unroll 1
+    for (int j0 = 0; j0 < kFeat; j0 += 8) {
+        uint32_t sp[4], cp[4];
+#pragma unroll
+        for (int q = 0; q < 8; q += 2) {
+            float s0, c0, s1, c1;
+            const int j = j0 + q;
+            const uint32_t ph0 = (uint32_t)fs[3 * j] * U0 + (uint32_t)fs[3 * j + 1] * U1 + (uint32_t)fs[3 * j + 2] * U2;
+            const uint32_t ph1 = (uint32_t)fs[3 * j + 3] * U0 + (uint32_t)fs[3 * j + 4] * U1 +
+                                 (uint32_t)fs[3 * j + 5] * U2;
+            __sincosf(mixed::rev_to_rad(ph0), &s0, &c0);
+            __sincosf(mixed::rev_to_rad(ph1), &s1, &c1);
+            sp[q / 2] = pack_bf16(s0, s1);
+            cp[q / 2] = pack_bf16(c0, c1);
+        }
+        row[j0 / 8] = make_uint4(sp[0], sp[1], sp[2], sp[3]);
+        row[(kFeat + j0) / 8] = make_uint4(cp[0], cp[1], cp[2], cp[3]);
+        if (XT) {
+            unsigned short* xt = reinterpret_cast<unsigned short*>(XT);
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                xt[(size_t)(j0 + q) * n + i] = (unsigned short)(sp[q / 2] >> (16 * (q & 1)));
+                xt[(size_t)(kFeat + j0 + q) * n + i] = (unsigned short)(cp[q / 2] >> (16 * (q & 1)));
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------- samples
@@ -97,7 +111,8 @@ __global__ void samples_kernel(uint64_t seed, long long first, int n, const tp_m
 
 // ---------------------------------------------------------------- loss, biases, AdamW
 // dY = 2 (y - t_n) / (n * 6) with t_n the normalised target; BF16 dY padded with
-// zeros to kDYld columns (one k-atom of the output layer's data-gradient GEMM)
+// zeros to kDYld columns (one k-atom of the output layer's data-gradient GEMM);
+// the kernel writes the first 8, the rest are zeroed once
 constexpr int kDYld = 64;
 constexpr int kWgradSplits = 80;  // most split-K parts of a weight-gradient GEMM
 __global__ void loss_kernel(const float* __restrict__ Y, const float* __restrict__ T, int n,
@@ -109,16 +124,16 @@ __global__ void loss_kernel(const float* __restrict__ Y, const float* __restrict
     float l = 0.f;
     if (i < n) {
         const float scale = 2.0f / ((float)n * kOut);
-        for (int c = 0; c < kDYld; c++) {
-            float g = 0.f;
-            if (c < kOut) {
-                float r = Y[(size_t)i * kOut + c] - (T[(size_t)i * kOut + c] - mean[c]) * istd[c];
-                l += r * r;
-                g = r * scale;
-                if (dYf) dYf[(size_t)i * kOut + c] = g;
-            }
-            dY[(size_t)i * kDYld + c] = __float2bfloat16(g);
+        float g[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int c = 0; c < kOut; c++) {
+            float r = Y[(size_t)i * kOut + c] - (T[(size_t)i * kOut + c] - mean[c]) * istd[c];
+            l += r * r;
+            g[c] = r * scale;
+            if (dYf) dYf[(size_t)i * kOut + c] = g[c];
         }
+        // columns 8.. of dY stay zero from its allocation (mlp_reserve)
+        *reinterpret_cast<uint4*>(dY + (size_t)i * kDYld) =
+            make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], g[3]), pack_bf16(g[4], g[5]), pack_bf16(g[6], g[7]));
     }
     for (int off = 16; off > 0; off >>= 1) l += __shfl_down_sync(0xffffffffu, l, off);
     if ((threadIdx.x & 31) == 0) atomicAdd(loss, (double)l);
@@ -131,11 +146,16 @@ __global__ void loss_kernel(const float* __restrict__ Y, const float* __restrict
 __global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ GT, int n, float* __restrict__ db)
 {
     __shared__ float red[8];
-    const __nv_bfloat162* row = reinterpret_cast<const __nv_bfloat162*>(GT + (size_t)blockIdx.x * n);
+    const uint4* row = reinterpret_cast<const uint4*>(GT + (size_t)blockIdx.x * n);
     float s = 0.f;
-    for (int i = threadIdx.x; i < n / 2; i += blockDim.x) {
-        const float2 v = __bfloat1622float2(row[i]);
-        s += v.x + v.y;
+    for (int i = threadIdx.x; i < n / 8; i += blockDim.x) {  // 8 values per 16-byte load
+        const uint4 v = row[i];
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[q]));
+            s += f.x + f.y;
+        }
     }
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
@@ -152,7 +172,7 @@ __global__ void bias_grad_kernel(const __nv_bfloat16* __restrict__ GT, int n, fl
 // db4[o] += sum_r dYf[r][o].  A block takes kOutRows consecutive samples:
 // thread k owns column k of H3 and keeps six sums; FP32 atomics add the
 // block's partial sums.
-constexpr int kOutRows = 512;
+constexpr int kOutRows = 128;
 __global__ void __launch_bounds__(256) out_grad_kernel(const float* __restrict__ dYf,
                                                        const __nv_bfloat16* __restrict__ H3, int n,
                                                        float* __restrict__ dW4, float* __restrict__ db4)
@@ -302,6 +322,8 @@ static bool mlp_reserve(int n)
     for (int l = 0; l < 4 && ok; l++)
         ok = cuda_ok(cudaMalloc(&M.Z[l], h), "Z") && cuda_ok(cudaMalloc(&M.H[l], h), "H") &&
              cuda_ok(cudaMalloc(&M.HT[l], h), "HT");
+    // the padding columns of dY (beyond the 8 the loss kernel writes) stay zero
+    if (ok) ok = cuda_ok(cudaMemsetAsync(M.dY, 0, sizeof(__nv_bfloat16) * (size_t)n * kDYld, g.stream), "dY zero");
     if (ok) M.cap = n;
     return ok;
 }
