@@ -19,6 +19,7 @@
 // Long K ranges (the weight gradients) use 4 stages; short ones (K <= 256:
 // four atoms) use 2, which halves the shared memory so that two CTAs share
 // an SM and one's epilogue overlaps the other's copies and MMAs.
+#include <algorithm>
 #include <cstdint>
 
 #include "../../include/tp_gpu.h"
@@ -192,7 +193,8 @@ static cudaError_t launch(const __nv_bfloat16* A, int lda, const __nv_bfloat16* 
 struct EpiStoreF32 {  // D[m][n] = acc (self-check)
     float* D;
     int ld;
-    __device__ void begin(int) {}
+    template <int CW = 256>
+    __device__ void begin(int, int = 0) {}
     __device__ void operator()(int m, int c0, const float* v, int cnt) const
     {
         for (int i = 0; i < cnt; i++) D[(size_t)m * ld + c0 + i] = v[i];
@@ -204,7 +206,8 @@ struct EpiHiddenT {
     const float* b;
     __nv_bfloat16 *Z, *H, *HT;
     int M;
-    __device__ void begin(int) {}
+    template <int CW = 256>
+    __device__ void begin(int, int = 0) {}
     __device__ void operator()(int m, int c0, const float* v, int cnt) const
     {
 #pragma unroll
@@ -232,7 +235,8 @@ struct EpiHiddenT {
 struct EpiOutT {
     const float* b;
     float* Y;
-    __device__ void begin(int) {}
+    template <int CW = 256>
+    __device__ void begin(int, int = 0) {}
     __device__ void operator()(int m, int c0, const float* v, int cnt) const
     {
         for (int c = 0; c < mlp::kOut; c++) Y[(size_t)m * mlp::kOut + c] = v[c] + b[c];
@@ -246,17 +250,21 @@ struct EpiBackSiluT {
     __nv_bfloat16 *G, *GT;
     int M;
     uint4 zrow[mlp::kHid / 8];
-    __device__ void begin(int m)
+    int zc0 = 0;  // first column of the preloaded window
+    // preloads columns [c0, c0 + CW) of row m
+    template <int CW = mlp::kHid>
+    __device__ void begin(int m, int c0 = 0)
     {
-        const uint4* src = reinterpret_cast<const uint4*>(Z + (size_t)m * mlp::kHid);
+        zc0 = c0;
+        const uint4* src = reinterpret_cast<const uint4*>(Z + (size_t)m * mlp::kHid + c0);
 #pragma unroll
-        for (int i = 0; i < mlp::kHid / 8; i++) zrow[i] = __ldg(src + i);
+        for (int i = 0; i < CW / 8; i++) zrow[i] = __ldg(src + i);
     }
     __device__ void operator()(int m, int c0, const float* v, int cnt) const
     {
 #pragma unroll
         for (int i = 0; i < 32; i += 8) {
-            const uint4 zr = zrow[(c0 + i) / 8];
+            const uint4 zr = zrow[(c0 - zc0 + i) / 8];
             const uint32_t zw[4] = {zr.x, zr.y, zr.z, zr.w};
             uint32_t gp[4];
 #pragma unroll
@@ -281,7 +289,8 @@ struct EpiBackSiluT {
 struct EpiPartial {
     float* P;
     int M, N;
-    __device__ void begin(int) {}
+    template <int CW = 256>
+    __device__ void begin(int, int = 0) {}
     __device__ void operator()(int m, int c0, const float* v, int cnt) const
     {
         float* dst = P + ((size_t)blockIdx.y * M + m) * N + c0;
@@ -300,15 +309,228 @@ __global__ void reduce_partials_kernel(const float* __restrict__ P, int splits, 
     gr[i] += s;
 }
 
+// ---------------------------------------------------------------- persistent, warp-specialised
+// The forward and data-gradient GEMMs (N = 256, K <= 256) as a persistent
+// kernel with one role per warp, one CTA per SM walking 128-row tiles:
+//   warp 0  producer: the whole B operand (the layer's weights, N x K) once
+//           into shared memory, where it stays; then the A k-atoms of every
+//           tile through a ring of kWsRing stages with 16-byte cp.async, up to
+//           kWsAhead atoms in flight, each signalled on its stage's `full`;
+//   warp 1  MMA: one thread issues the four K = 16 MMAs per atom into one of
+//           two 256-column accumulators in tensor memory (alternating per
+//           tile), frees the stage on `empty` and signals `accf` per tile;
+//   warps 2.. epilogue (kWsEpiWarps of them, up to four per quadrant of
+//           tensor-memory lanes, each taking a slice of the columns): each
+//           reads its 32 accumulator lanes (rows) of a finished tile and
+//           signals `acce` when its part of the buffer is drained.
+// So a tile's epilogue overlaps the next tile's copies and MMAs.  Every wait
+// is bounded; one that runs out sets the block's abort flag, every other wait
+// then gives up, the block drains its MMAs (bounded), frees tensor memory and
+// raises ST_TIMEOUT.
+#ifndef TP_TCT_EPI_WARPS
+#define TP_TCT_EPI_WARPS 8
+#endif
+constexpr int kWsEpiWarps = TP_TCT_EPI_WARPS;  // 4, 8 or 16: 1, 2 or 4 per tensor-memory lane quadrant
+constexpr int kWsThreads = 64 + 32 * kWsEpiWarps;
+constexpr int kWsCols = 256 * 4 / kWsEpiWarps;  // accumulator columns per epilogue warp
+constexpr int kWsRing = 4;
+constexpr int kWsAhead = 2;
+constexpr uint32_t kWsLimit = 1u << 22;
+
+__device__ __forceinline__ bool ws_wait(uint32_t bar, uint32_t parity, volatile int* abort)
+{
+    for (uint32_t it = 0; it < kWsLimit; it++) {
+        if (tc::mbar_try_wait(bar, parity)) return true;
+        if ((it & 63u) == 63u && *abort) return false;
+    }
+    *abort = 1;
+    return false;
+}
+
+size_t ws_smem_bytes(int k) { return 1024 + (size_t)(k / 64) * 256 * 128 + (size_t)kWsRing * a_stage_bytes(); }
+
+template <class Epi>
+__global__ void __launch_bounds__(kWsThreads, 1) tcgemm_ws_kernel(const __nv_bfloat16* __restrict__ A, int lda,
+                                                                  const __nv_bfloat16* __restrict__ B, int ldb,
+                                                                  int M, int K, Epi epi, int* __restrict__ status)
+{
+    constexpr int N = 256;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bars[2 * kWsRing + 6];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int katoms = K / 64, ntiles = M / 128;
+    const uint32_t raw = tc::smem_addr(smem_raw);
+    const uint32_t sB = raw + ((1024u - (raw & 1023u)) & 1023u);
+    const uint32_t sA = sB + (uint32_t)katoms * N * 128u;
+    const uint32_t bar0 = tc::smem_addr(&bars[0]);
+    auto full = [&](int st) { return bar0 + 8u * st; };
+    auto empty = [&](int st) { return bar0 + 8u * (kWsRing + st); };
+    const uint32_t bfull = bar0 + 8u * (2 * kWsRing);
+    auto accf = [&](int b) { return bar0 + 8u * (2 * kWsRing + 1 + b); };
+    auto acce = [&](int b) { return bar0 + 8u * (2 * kWsRing + 3 + b); };
+    const uint32_t fin = bar0 + 8u * (2 * kWsRing + 5);
+    volatile int* abort = &abort_flag;
+    if (tid == 0) {
+        for (int st = 0; st < kWsRing; st++) {
+            tc::mbar_init(full(st), 32);
+            tc::mbar_init(empty(st), 1);
+        }
+        tc::mbar_init(bfull, 32);
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(accf(b), 1);
+            tc::mbar_init(acce(b), 32 * kWsEpiWarps);
+        }
+        tc::mbar_init(fin, 1);
+        tc::mbar_fence_init();
+        abort_flag = 0;
+    }
+    if (warp == 1) {
+        tc::tmem_alloc(tc::smem_addr(&tmem_slot), 512);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        // B, resident for every tile of this block
+        for (int c = lane; c < katoms * N * 8; c += 32) {
+            const int a = c / (N * 8), rem = c % (N * 8), r = rem >> 3, kk = (rem & 7) * 8;
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+                         ::"r"(sB + (uint32_t)a * N * 128u + tc::sw128_offset(N, r, kk)),
+                         "l"(B + (size_t)r * ldb + a * 64 + kk)
+                         : "memory");
+        }
+        asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+        tc::fence_async_smem();
+        tc::mbar_arrive(bfull);
+        // A atoms of every tile through the ring
+        uint32_t u = 0;
+        bool ok = true;
+        for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+            const int m0 = t * 128;
+            for (int a = 0; ok && a < katoms; a++, u++) {
+                const int st = (int)(u % kWsRing);
+                const uint32_t use = u / kWsRing;
+                if (use > 0) ok = ws_wait(empty(st), (use - 1) & 1u, abort);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) break;
+                const uint32_t dst = sA + (uint32_t)st * a_stage_bytes();
+                for (int c = lane; c < 128 * 8; c += 32) {
+                    const int r = c >> 3, kk = (c & 7) * 8;
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+                                 ::"r"(dst + tc::sw128_offset(128, r, kk)),
+                                 "l"(A + (size_t)(m0 + r) * lda + a * 64 + kk)
+                                 : "memory");
+                }
+                asm volatile("cp.async.commit_group;" ::: "memory");
+                if (u >= (uint32_t)kWsAhead) {  // the atom kWsAhead behind has landed
+                    asm volatile("cp.async.wait_group %0;" ::"n"(kWsAhead) : "memory");
+                    tc::fence_async_smem();
+                    tc::mbar_arrive(full((int)((u - kWsAhead) % kWsRing)));
+                }
+            }
+        }
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        if (ok) {
+            tc::fence_async_smem();
+            for (uint32_t w = u >= (uint32_t)kWsAhead ? u - kWsAhead : 0; w < u; w++)
+                tc::mbar_arrive(full((int)(w % kWsRing)));
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && ws_wait(bfull, 0, abort)) {
+            tc::tc_fence_after();
+            const uint32_t idesc = tc::idesc_bf16_f32(128, N);
+            uint32_t u = 0, j = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < ntiles; t += gridDim.x, j++) {
+                const int b = (int)(j & 1u);
+                const uint32_t v = j >> 1;
+                if (v > 0) ok = ws_wait(acce(b), (v - 1) & 1u, abort);
+                if (!ok) break;
+                tc::tc_fence_after();
+                for (int a = 0; ok && a < katoms; a++, u++) {
+                    const int st = (int)(u % kWsRing);
+                    ok = ws_wait(full(st), (u / kWsRing) & 1u, abort);
+                    if (!ok) break;
+                    tc::tc_fence_after();
+                    const uint64_t ad = tc::desc_sw128(sA + (uint32_t)st * a_stage_bytes());
+                    const uint64_t bd = tc::desc_sw128(sB + (uint32_t)a * N * 128u);
+#pragma unroll
+                    for (int kk = 0; kk < 4; kk++)
+                        tc::mma_bf16(tmem + (uint32_t)(b * N), ad + 2 * kk, bd + 2 * kk, idesc, (a | kk) != 0);
+                    tc::mma_commit(empty(st));
+                }
+                if (ok) tc::mma_commit(accf(b));
+            }
+        }
+        __syncwarp();
+    } else {
+        const int q = warp & 3;  // the tensor-memory lanes this warp may read
+        const int cbase = ((warp - 2) >> 2) * kWsCols;  // its slice of the columns
+        const uint32_t lane_base = (uint32_t)(32 * q) << 16;
+        uint32_t j = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, j++) {
+            const int b = (int)(j & 1u);
+            const int row = t * 128 + 32 * q + lane;
+            Epi e = epi;
+            e.template begin<kWsCols>(row, cbase);
+            if (!ws_wait(accf(b), (j >> 1) & 1u, abort)) break;
+            tc::tc_fence_after();
+#pragma unroll
+            for (int c = 0; c < kWsCols; c += 32) {
+                float vals[32];
+                tc::tmem_ld32(tmem + lane_base + (uint32_t)(b * N + cbase + c), vals);
+                e(row, cbase + c, vals, 32);
+            }
+            tc::tc_fence_before();
+            tc::mbar_arrive(acce(b));
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        if (lane == 0) {  // every MMA this block issued has completed (bounded)
+            tc::mma_commit(fin);
+            if (!tc::mbar_wait(fin, 0, kWsLimit)) abort_flag = 1;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    if (tid == 0 && abort_flag) atomicOr(status, ST_TIMEOUT);
+    if (warp == 1) tc::tmem_dealloc(tmem, 512);
+}
+
+template <class Epi>
+static cudaError_t launch_ws(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M, int K,
+                             const Epi& epi, int* status, cudaStream_t s)
+{
+    if (M % 128 || K % 64 || K < 64 || K > 256) return cudaErrorInvalidValue;
+    const size_t smem = ws_smem_bytes(K);
+    cudaError_t e = cudaFuncSetAttribute(tcgemm_ws_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    const int grid = std::min(M / 128, g.num_sms > 0 ? g.num_sms : 148);
+    tcgemm_ws_kernel<Epi><<<grid, kWsThreads, smem, s>>>(A, lda, B, ldb, M, K, epi, status);
+    return cudaGetLastError();
+}
+
 }  // namespace tct
 
 namespace tctrain {
 
 using namespace tct;
 
+#ifndef TP_TCT_WS
+#define TP_TCT_WS 1
+#endif
+
 cudaError_t forward_hidden(const __nv_bfloat16* X, int lda, const __nv_bfloat16* W, int kin, int M, const float* b,
                            __nv_bfloat16* Z, __nv_bfloat16* H, __nv_bfloat16* HT, int* status, cudaStream_t s)
 {
+    if (TP_TCT_WS) return launch_ws(X, lda, W, kin, M, kin, EpiHiddenT{b, Z, H, HT, M}, status, s);
     return launch(X, lda, W, kin, M, mlp::kHid, kin, 1, EpiHiddenT{b, Z, H, HT, M}, status, s);
 }
 
@@ -322,6 +544,7 @@ cudaError_t backward_data(const __nv_bfloat16* Gin, int ldg, const __nv_bfloat16
                           const __nv_bfloat16* Zprev, __nv_bfloat16* G, __nv_bfloat16* GT, int* status,
                           cudaStream_t s)
 {
+    if (TP_TCT_WS) return launch_ws(Gin, ldg, WT, kout, M, kout, EpiBackSiluT{Zprev, G, GT, M}, status, s);
     return launch(Gin, ldg, WT, kout, M, mlp::kHid, kout, 1, EpiBackSiluT{Zprev, G, GT, M}, status, s);
 }
 
@@ -342,6 +565,8 @@ cudaError_t backward_weights(const __nv_bfloat16* GT, const __nv_bfloat16* XT, i
 cudaError_t gemm_f32(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K, float* D, int* status,
                      cudaStream_t s)
 {
+    // the shapes of the forward and data-gradient GEMMs go through the kernel those use
+    if (TP_TCT_WS && N == 256 && K <= 256) return launch_ws(A, K, B, K, M, K, EpiStoreF32{D, N}, status, s);
     return launch(A, K, B, K, M, N, K, 1, EpiStoreF32{D, N}, status, s);
 }
 

@@ -39,10 +39,13 @@ def test_tile_gemm_matches_fp64(n, k):
 
 
 @pytest.mark.parametrize("m,n,k", [(128, 256, 256), (256, 16, 256), (384, 128, 640), (256, 256, 64),
-                                   (128, 48, 4096)])
+                                   (128, 48, 4096), (640 * 128, 256, 256), (1024, 256, 128)])
 def test_training_gemm_matches_fp64(m, n, k):
-    """The training GEMM kernel (ring of k-atoms through shared memory, one
-    tcgen05.mma chain per 128-row tile) over several tiles and long K."""
+    """The training GEMM kernels: the ring of k-atoms through shared memory
+    with one tcgen05.mma chain per 128-row tile (several tiles, long K), and,
+    for N = 256 and K <= 256, the persistent warp-specialised kernel (B
+    resident, two accumulators in tensor memory; 640 tiles: several per
+    block, both accumulators reused)."""
     rng = np.random.default_rng(m * 7 + n * 1000 + k)
     a = bf16_bits(rng.uniform(-1, 1, size=(m, k)))
     b = bf16_bits(rng.uniform(-1, 1, size=(n, k)))
