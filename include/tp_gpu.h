@@ -306,8 +306,8 @@ int tp_tc_gemm_train_bf16(int m, int n, int k, const unsigned short *a, const un
  * src/poincare_map.c:101-181 for a batch of seeds. */
 int tp_poincare_trace(int n, const double *seeds, int face, double step, double length_max, int ncross,
                       double *xpos, double *ypos, double *zpos, int *found);
-/* Writer used by poincare_map (weak; the default writes data/poincare_map.bin,
- * see poincare.cu).  Define it to write the reference's HDF5 file instead. */
+/* Writer used by poincare_map (weak; the default writes the reference's
+ * data/poincare_map.h5 through tp_h5_write_poincare, tp_h5.h). */
 void tp_poincare_save(int mpi_rank, int mpi_size, int npoints_total, int ncross, int nshift,
                       int npoints, const double *xpos, const double *ypos, const double *zpos);
 

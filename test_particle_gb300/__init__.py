@@ -415,3 +415,59 @@ def fetch_device_fields():
     hb = np.zeros((n, 3), dtype=np.float32)
     check(L.tp_fetch_device_fields(_ptr(he), _ptr(hb)), "fetch_device_fields")
     return he, hb
+
+
+# ---------------------------------------------------------------- HDF5 files (no libhdf5)
+def read_pic_fields_h5(fname, gname, with_e=True):
+    """Load the [nx][ny][nz] datasets cbx, cby, cbz (and ex, ey, ez) of group
+    gname into device memory, transposed to the reference's x-fastest records
+    and scaled by B0 / E0 (tp_read_pic_fields_h5; the reference's
+    read_pic_bfields_h5 / read_pic_efields_h5)."""
+    check(lib().tp_read_pic_fields_h5(str(fname).encode(), str(gname).encode(), C.c_int(1 if with_e else 0)),
+          "read_pic_fields_h5")
+
+
+def h5_info(fname, gname, dset):
+    """(dims, type class, type size) of dataset gname/dset (tp_h5_info)."""
+    rank, cls, size = C.c_int(), C.c_int(), C.c_int()
+    dims = (C.c_ulonglong * 32)()
+    check(lib().tp_h5_info(str(fname).encode(), str(gname).encode(), str(dset).encode(), C.byref(rank), dims,
+                           C.byref(cls), C.byref(size)), "h5_info")
+    return tuple(dims[i] for i in range(rank.value)), cls.value, size.value
+
+
+def h5_read(fname, gname, dset, offset=None, count=None, dtype=np.float64):
+    """The hyperslab [offset, offset + count) of a numeric dataset as float64
+    or float32 (tp_h5_read; the whole dataset by default)."""
+    dims, _, _ = h5_info(fname, gname, dset)
+    offset = [0] * len(dims) if offset is None else list(offset)
+    count = [d - o for d, o in zip(dims, offset)] if count is None else list(count)
+    dt = np.dtype(dtype)
+    out = np.zeros(count, dtype=dt)
+    r = len(dims)
+    check(lib().tp_h5_read(str(fname).encode(), str(gname).encode(), str(dset).encode(), C.c_int(r),
+                           (C.c_ulonglong * max(r, 1))(*count), (C.c_ulonglong * max(r, 1))(*offset),
+                           C.c_int(dt.itemsize), _ptr(out)), "h5_read")
+    return out
+
+
+def save_particles_fields(fname, ptl, ntot=None, offset=0):
+    """Write records [offset, offset + len(ptl)) of a particles_fields file of
+    ntot records (default len(ptl)), with the fields at each record from the
+    library's FP64 get_emf on the GPU (tp_save_particles_fields); the writer
+    of the records at offset 0 also writes the file's metadata."""
+    p = np.ascontiguousarray(ptl, dtype=PARTICLE_DTYPE)
+    ntot = len(p) if ntot is None else int(ntot)
+    acc = np.array([offset], dtype=np.int32)
+    check(lib().tp_save_particles_fields(C.c_int(1 if offset else 0), C.c_int(len(p)), _ptr(p), C.c_int(ntot),
+                                         _ptr(acc), str(fname).encode(), C.c_int(0)), "save_particles_fields")
+
+
+def read_particles(fname, n, offset=0):
+    """Records [offset, offset + n) of /particles_fields/particles
+    (tp_read_particles); the shifts are zero."""
+    p = np.zeros(n, dtype=PARTICLE_DTYPE)
+    acc = np.array([offset], dtype=np.int32)
+    check(lib().tp_read_particles(C.c_int(1 if offset else 0), C.c_int(n), _ptr(acc), _ptr(p),
+                                  str(fname).encode()), "read_particles")
+    return p

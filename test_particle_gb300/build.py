@@ -37,6 +37,8 @@ UNITS = [
     ("tc_train.o", "tc_train.cu", []),
     ("poincare.o", "poincare.cu", []),
     ("loaders.o", "loaders.cu", []),
+    ("h5lite.o", "h5lite.cpp", []),
+    ("h5io.o", "h5io.cu", []),
 ]
 
 

@@ -1,0 +1,322 @@
+// h5io.cu -- the reference's HDF5 files read and written by the library
+// (h5lite.cpp), without libhdf5.
+//
+//   read_data_serial_{double,float}_h5, read_data_serial_{float,double}_binary:
+//       the reference's data_io.c (src/data_io.c:22-120) with its signatures,
+//       so a program linked against this library needs no data_io.o and no
+//       libhdf5 to read its field files;
+//   tp_h5_read / tp_h5_info: the same reads with an error status;
+//   tp_save_particles_fields / tp_read_particles: particles_fields_init.h5 and
+//       particle_diagnostics.h5 (src/diagnostics.c:290-387,
+//       src/particle_info.c:376-488), the fields at the particles evaluated on
+//       the GPU by the library's FP64 get_emf;
+//   tp_h5_write_particles_fields: the writer alone, with the fields given;
+//   tp_h5_write_poincare: data/poincare_map.h5 (src/poincare_map.c:185-235).
+// Several ranks writing one file each call with their own records: the file's
+// layout depends only on the totals, so the rank holding the first record
+// writes the metadata and every rank writes its records where they belong,
+// with no exchange; the file is complete once every rank has returned.
+#include <fcntl.h>
+#include <unistd.h>
+
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/tp_gpu.h"
+#include "../../include/tp_h5.h"
+#include "h5lite.h"
+#include "tp_internal.h"
+
+using namespace tp;
+
+namespace {
+
+const std::vector<std::string> kPtlNames = {"x", "y", "z", "qm", "ux", "uy", "uz", "t"};
+const std::vector<std::string> kEmfNames = {"Bx", "By", "Bz", "Ex", "Ey", "Ez"};
+
+// The two datasets of a particles_fields file of ntot records.
+tph5::Plan particles_plan(unsigned long long ntot)
+{
+    tph5::Plan p;
+    tph5::WGroup g;
+    g.name = "particles_fields";
+    g.dsets.push_back({"particles", tph5::Type::compound_f64(kPtlNames, true), {ntot}});
+    g.dsets.push_back({"fields", tph5::Type::compound_f64(kEmfNames, true), {ntot}});
+    p.groups.push_back(g);
+    p.plan();
+    return p;
+}
+
+struct Fd {
+    int fd = -1;
+    ~Fd()
+    {
+        if (fd >= 0) close(fd);
+    }
+};
+
+bool h5_read_as(const char* fname, const char* gname, const char* dset, int rank, const unsigned long long* count,
+                const unsigned long long* offset, int elem_bytes, void* data)
+{
+    if (!fname || !dset || rank < 0 || rank > 32 || (rank > 0 && (!count || !offset)) ||
+        (elem_bytes != 4 && elem_bytes != 8)) {
+        set_error(7, "tp_h5_read: bad arguments");
+        return false;
+    }
+    tph5::File f;
+    tph5::Dataset ds;
+    if (!f.open(fname) || !f.dataset(gname, dset, ds)) {
+        set_error(7, "%s", f.error().c_str());
+        return false;
+    }
+    if ((int)ds.dims.size() != rank) {
+        set_error(7, "%s: dataset '%s' has rank %zu, not %d", fname, dset, ds.dims.size(), rank);
+        return false;
+    }
+    if (ds.type.cls != 0 && ds.type.cls != 1) {
+        set_error(7, "%s: dataset '%s' is not of a numeric type", fname, dset);
+        return false;
+    }
+    uint64_t n = 1;
+    std::vector<uint64_t> o(rank), c(rank);
+    for (int d = 0; d < rank; d++) {
+        o[d] = offset[d];
+        c[d] = count[d];
+        n *= c[d];
+    }
+    std::vector<uint8_t> raw(n * ds.type.size);
+    if (!f.read(ds, o.data(), c.data(), raw.data())) {
+        set_error(7, "%s", f.error().c_str());
+        return false;
+    }
+    if (elem_bytes == 8) tph5::raw_to_double(ds.type, raw.data(), n, (double*)data);
+    else tph5::raw_to_float(ds.type, raw.data(), n, (float*)data);
+    return true;
+}
+
+}  // namespace
+
+extern "C" int tp_h5_read(const char* fname, const char* gname, const char* dset, int rank,
+                          const unsigned long long* count, const unsigned long long* offset, int elem_bytes,
+                          void* data)
+{
+    return h5_read_as(fname, gname, dset, rank, count, offset, elem_bytes, data) ? 0 : -1;
+}
+
+extern "C" int tp_h5_info(const char* fname, const char* gname, const char* dset, int* rank,
+                          unsigned long long* dims, int* type_class, int* type_size)
+{
+    tph5::File f;
+    tph5::Dataset ds;
+    if (!fname || !dset || !f.open(fname) || !f.dataset(gname, dset, ds)) {
+        set_error(7, "%s", fname ? f.error().c_str() : "tp_h5_info: no file name");
+        return -1;
+    }
+    if (ds.dims.size() > 32) {
+        set_error(7, "%s: rank above 32", fname);
+        return -1;
+    }
+    if (rank) *rank = (int)ds.dims.size();
+    if (dims)
+        for (size_t d = 0; d < ds.dims.size(); d++) dims[d] = ds.dims[d];
+    if (type_class) *type_class = ds.type.cls;
+    if (type_size) *type_size = (int)ds.type.size;
+    return 0;
+}
+
+// src/data_io.c:22-47 and :52-75.  libhdf5 prints its error stack and the
+// reference carries on; these print the reason and leave data untouched.
+extern "C" void read_data_serial_double_h5(int rank, unsigned long long* count, unsigned long long* offset,
+                                           char* fname, char* gname, char* dset_name, double* data)
+{
+    if (!h5_read_as(fname, gname, dset_name, rank, count, offset, 8, data)) fprintf(stderr, "HDF5 read: %s\n", g.err);
+}
+
+extern "C" void read_data_serial_float_h5(int rank, unsigned long long* count, unsigned long long* offset,
+                                          char* fname, char* gname, char* dset_name, float* data)
+{
+    if (!h5_read_as(fname, gname, dset_name, rank, count, offset, 4, data)) fprintf(stderr, "HDF5 read: %s\n", g.err);
+}
+
+// src/data_io.c:90-120: the file's values from element `offset` on.
+template <class T>
+static void read_binary(const char* fname, long offset, long size, T* data)
+{
+    FILE* fp = fopen(fname, "r");
+    if (!fp) {
+        printf("Unable to open file %s!\n", fname);
+        exit(1);
+    }
+    fseek(fp, offset * (long)sizeof(T), SEEK_SET);
+    size_t got = fread(data, sizeof(T), (size_t)size, fp);
+    (void)got;  // a short file leaves the rest untouched, as the reference
+    fclose(fp);
+}
+
+extern "C" void read_data_serial_float_binary(char* fname, long offset, long size, float* data)
+{
+    read_binary(fname, offset, size, data);
+}
+
+extern "C" void read_data_serial_double_binary(char* fname, long offset, long size, double* data)
+{
+    read_binary(fname, offset, size, data);
+}
+
+extern "C" int tp_h5_write_particles_fields(const char* fname, int write_meta, unsigned long long ntot,
+                                            unsigned long long offset, int nptl, const particles* ptl,
+                                            const emfields* emf)
+{
+    if (!fname || nptl < 0 || offset + (unsigned long long)nptl > ntot || (nptl > 0 && (!ptl || !emf))) {
+        set_error(7, "tp_h5_write_particles_fields: bad arguments");
+        return -1;
+    }
+    tph5::Plan p = particles_plan(ntot);
+    std::string err;
+    Fd fd;
+    fd.fd = tph5::open_for_write(fname, err);
+    if (fd.fd < 0 || (write_meta && !tph5::write_meta(fd.fd, p, err))) {
+        set_error(7, "%s", err.c_str());
+        return -1;
+    }
+    const tph5::WDataset* dp = p.find("particles_fields", "particles");
+    const tph5::WDataset* de = p.find("particles_fields", "fields");
+    constexpr int kBlock = 65536;
+    std::vector<uint8_t> buf((size_t)kBlock * 64);
+    for (int i0 = 0; i0 < nptl; i0 += kBlock) {
+        const int m = nptl - i0 < kBlock ? nptl - i0 : kBlock;
+        for (int i = 0; i < m; i++) {
+            const particles& q = ptl[i0 + i];
+            const double v[8] = {q.x, q.y, q.z, q.qm, q.ux, q.uy, q.uz, q.t};
+            for (int c = 0; c < 8; c++) tph5::put_f64(&buf[64 * (size_t)i + 8 * c], v[c], true);
+        }
+        if (!tph5::write_elements(fd.fd, *dp, offset + i0, m, buf.data(), err)) break;
+        for (int i = 0; i < m; i++) {
+            const emfields& q = emf[i0 + i];
+            const double v[6] = {q.Bx, q.By, q.Bz, q.Ex, q.Ey, q.Ez};
+            for (int c = 0; c < 6; c++) tph5::put_f64(&buf[48 * (size_t)i + 8 * c], v[c], true);
+        }
+        if (!tph5::write_elements(fd.fd, *de, offset + i0, m, buf.data(), err)) break;
+    }
+    if (!err.empty()) {
+        set_error(7, "%s: %s", fname, err.c_str());
+        return -1;
+    }
+    return 0;
+}
+
+// save_particles_fields, src/diagnostics.c:290-387: this rank's nptl records
+// at offset naccumulate[mpi_rank - 1] (0 for rank 0) of ntot, with the fields
+// at each record's (x, y, z, t) from the library's FP64 get_emf.
+extern "C" int tp_save_particles_fields(int mpi_rank, int nptl, particles* ptl, int ntot, int* naccumulate,
+                                        char* fname, int system_type_arg)
+{
+    (void)system_type_arg;  // the reference passes it through unused
+    if (mpi_rank < 0 || nptl < 0 || ntot < 0 || (mpi_rank > 0 && !naccumulate)) {
+        set_error(7, "tp_save_particles_fields: bad arguments");
+        return -1;
+    }
+    const unsigned long long off = mpi_rank == 0 ? 0ull : (unsigned long long)naccumulate[mpi_rank - 1];
+    std::vector<emfields> emf((size_t)nptl);
+    if (nptl > 0) {
+        std::vector<double> xyzt(4 * (size_t)nptl);
+        for (int i = 0; i < nptl; i++) {
+            xyzt[4 * (size_t)i] = ptl[i].x;
+            xyzt[4 * (size_t)i + 1] = ptl[i].y;
+            xyzt[4 * (size_t)i + 2] = ptl[i].z;
+            xyzt[4 * (size_t)i + 3] = ptl[i].t;
+        }
+        static_assert(sizeof(emfields) == 6 * sizeof(double), "emfields is six doubles");
+        if (tp_get_emf_batch(nptl, xyzt.data(), (double*)emf.data()) != 0) return -1;
+    }
+    return tp_h5_write_particles_fields(fname, off == 0, (unsigned long long)ntot, off, nptl, ptl, emf.data());
+}
+
+// read_particles, src/particle_info.c:376-443: records [offset, offset + nptl)
+// of /particles_fields/particles into x, y, z, qm, ux, uy, uz, t of ptl (the
+// other members are left as they are), converted from the file's type.
+extern "C" int tp_read_particles(int mpi_rank, int nptl, int* nptl_accumulate, particles* ptl, char* fname)
+{
+    if (mpi_rank < 0 || nptl < 0 || (mpi_rank > 0 && !nptl_accumulate) || !fname || (nptl > 0 && !ptl)) {
+        set_error(7, "tp_read_particles: bad arguments");
+        return -1;
+    }
+    tph5::File f;
+    tph5::Dataset ds;
+    if (!f.open(fname) || !f.dataset("/particles_fields", "particles", ds)) {
+        set_error(7, "%s", f.error().c_str());
+        return -1;
+    }
+    if (ds.dims.size() != 1 || ds.type.cls != 6) {
+        set_error(7, "%s: /particles_fields/particles is not a 1-D compound dataset", fname);
+        return -1;
+    }
+    const tph5::Member* mem[8] = {nullptr};
+    for (const tph5::Member& m : ds.type.members)
+        for (int c = 0; c < 8; c++)
+            if (m.name == kPtlNames[c]) {
+                if (m.type.cls < 0 || m.offset + m.type.size > ds.type.size) {
+                    set_error(7, "%s: member %s is not numeric", fname, m.name.c_str());
+                    return -1;
+                }
+                mem[c] = &m;
+            }
+    const uint64_t off = mpi_rank == 0 ? 0 : (uint64_t)nptl_accumulate[mpi_rank - 1];
+    constexpr uint64_t kBlock = 65536;
+    std::vector<uint8_t> raw(kBlock * ds.type.size);
+    for (uint64_t i0 = 0; i0 < (uint64_t)nptl; i0 += kBlock) {
+        uint64_t m = (uint64_t)nptl - i0 < kBlock ? (uint64_t)nptl - i0 : kBlock;
+        uint64_t o = off + i0;
+        if (!f.read(ds, &o, &m, raw.data())) {
+            set_error(7, "%s", f.error().c_str());
+            return -1;
+        }
+        for (uint64_t i = 0; i < m; i++) {
+            double* rec = (double*)&ptl[i0 + i];
+            const uint8_t* src = &raw[i * ds.type.size];
+            // particles: x, y, z, qm, ux, uy, uz, t are its first eight doubles
+            for (int c = 0; c < 8; c++)
+                if (mem[c]) rec[c] = tph5::decode(mem[c]->type, src + mem[c]->offset);
+        }
+    }
+    return 0;
+}
+
+// data/poincare_map.h5: /poincare_map/{xpos,ypos,zpos} [npoints_total][ncross + 1]
+// native doubles; this rank's rows [nshift, nshift + npoints).
+extern "C" int tp_h5_write_poincare(const char* fname, int npoints_total, int ncross, int nshift, int npoints,
+                                    const double* xpos, const double* ypos, const double* zpos)
+{
+    if (!fname || npoints_total < 0 || ncross < 0 || nshift < 0 || npoints < 0 || nshift + npoints > npoints_total ||
+        (npoints > 0 && (!xpos || !ypos || !zpos))) {
+        set_error(7, "tp_h5_write_poincare: bad arguments");
+        return -1;
+    }
+    tph5::Plan p;
+    tph5::WGroup g;
+    g.name = "poincare_map";
+    const std::vector<uint64_t> dims = {(uint64_t)npoints_total, (uint64_t)ncross + 1};
+    for (const char* n : {"xpos", "ypos", "zpos"}) g.dsets.push_back({n, tph5::Type::ieee(8, false), dims});
+    p.groups.push_back(g);
+    p.plan();
+    std::string err;
+    Fd fd;
+    fd.fd = tph5::open_for_write(fname, err);
+    if (fd.fd < 0 || (nshift == 0 && !tph5::write_meta(fd.fd, p, err))) {
+        set_error(7, "%s", err.c_str());
+        return -1;
+    }
+    const size_t m = (size_t)npoints * (ncross + 1);
+    std::vector<uint8_t> buf(8 * m);
+    const double* src[3] = {xpos, ypos, zpos};
+    for (int c = 0; c < 3 && err.empty(); c++) {
+        for (size_t i = 0; i < m; i++) tph5::put_f64(&buf[8 * i], src[c][i], false);
+        tph5::write_elements(fd.fd, p.groups[0].dsets[c], (uint64_t)nshift * (ncross + 1), m, buf.data(), err);
+    }
+    if (!err.empty()) {
+        set_error(7, "%s: %s", fname, err.c_str());
+        return -1;
+    }
+    return 0;
+}

@@ -1,0 +1,1009 @@
+// h5lite.cpp -- reader and writer of the HDF5 subset described in h5lite.h.
+//
+// Structures follow the HDF5 file format specification (superblock version
+// 0/1, object header version 1, symbol table / B-tree version 1 / local heap,
+// dataspace, datatype, fill value, layout and filter pipeline messages).  All
+// metadata integers are little-endian; offsets and lengths are 8 bytes.
+#include "h5lite.h"
+
+#include <fcntl.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cerrno>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+
+namespace tph5 {
+
+namespace {
+
+uint64_t le(const uint8_t* p, int n)
+{
+    uint64_t v = 0;
+    for (int i = n - 1; i >= 0; i--) v = (v << 8) | p[i];
+    return v;
+}
+
+uint64_t pad8(uint64_t n) { return (n + 7) & ~7ull; }
+
+// Bounds-checked cursor over a message body.
+struct Cur {
+    const uint8_t* p;
+    const uint8_t* end;
+    bool ok = true;
+    bool need(size_t n)
+    {
+        if (!ok || (size_t)(end - p) < n) ok = false;
+        return ok;
+    }
+    uint64_t u(int n)
+    {
+        if (!need(n)) return 0;
+        uint64_t v = le(p, n);
+        p += n;
+        return v;
+    }
+    void skip(size_t n)
+    {
+        if (need(n)) p += n;
+    }
+    std::string str(bool pad_to_8)
+    {
+        const uint8_t* s = p;
+        while (p < end && *p) p++;
+        if (p >= end) {
+            ok = false;
+            return std::string();
+        }
+        std::string r((const char*)s, (size_t)(p - s));
+        size_t used = (size_t)(p - s) + 1;
+        p = s;
+        skip(pad_to_8 ? pad8(used) : used);
+        return r;
+    }
+};
+
+// One datatype encoding (any class, so that unsupported members can be
+// skipped); atomic and compound types are filled in, others left as cls -1.
+bool parse_type(Cur& c, Type& t, int depth = 0)
+{
+    if (depth > 8 || !c.need(8)) return false;
+    const uint8_t cv = c.p[0];
+    const int cls = cv & 0x0f, ver = cv >> 4;
+    const uint32_t bits = (uint32_t)le(c.p + 1, 3);
+    const uint32_t size = (uint32_t)le(c.p + 4, 4);
+    c.skip(8);
+    t = Type();
+    t.size = size;
+    switch (cls) {
+    case 0: {  // fixed point: bit offset, precision
+        uint32_t off = (uint32_t)c.u(2), prec = (uint32_t)c.u(2);
+        if (off == 0 && prec == 8 * size && (size == 1 || size == 2 || size == 4 || size == 8)) {
+            t.cls = 0;
+            t.atom = Atomic{0, size, (bits & 1) != 0, (bits & 8) != 0};
+        }
+        break;
+    }
+    case 1: {  // floating point: IEEE binary32 / binary64 only
+        uint32_t off = (uint32_t)c.u(2), prec = (uint32_t)c.u(2);
+        uint32_t eloc = (uint32_t)c.u(1), esz = (uint32_t)c.u(1), mloc = (uint32_t)c.u(1), msz = (uint32_t)c.u(1);
+        uint32_t bias = (uint32_t)c.u(4);
+        const bool vax = (bits & 0x40) != 0;
+        const bool f32 = size == 4 && prec == 32 && eloc == 23 && esz == 8 && msz == 23 && bias == 127;
+        const bool f64 = size == 8 && prec == 64 && eloc == 52 && esz == 11 && msz == 52 && bias == 1023;
+        if (!vax && off == 0 && mloc == 0 && (f32 || f64)) {
+            t.cls = 1;
+            t.atom = Atomic{1, size, (bits & 1) != 0, true};
+        }
+        break;
+    }
+    case 2: c.skip(2); break;  // time
+    case 3: break;             // string
+    case 4: c.skip(4); break;  // bitfield
+    case 5: c.skip(bits & 0xff); break;  // opaque: tag
+    case 6: {  // compound
+        const int n = (int)(bits & 0xffff);
+        int offbytes = 1;
+        while (offbytes < 8 && (size >> (8 * offbytes)) != 0) offbytes++;
+        t.cls = 6;
+        for (int m = 0; m < n && c.ok; m++) {
+            Member mb;
+            mb.name = c.str(ver < 3);
+            if (ver < 3) {
+                mb.offset = (uint32_t)c.u(4);
+                if (ver == 1) {
+                    int dimensionality = (int)c.u(1);
+                    c.skip(3 + 4 + 4 + 16);
+                    if (dimensionality != 0) t.cls = -1;  // array members: not supported
+                }
+            } else {
+                mb.offset = (uint32_t)c.u(offbytes);
+            }
+            Type mt;
+            if (!parse_type(c, mt, depth + 1)) return false;
+            if (mt.cls == 0 || mt.cls == 1) mb.type = mt.atom;
+            t.members.push_back(mb);
+        }
+        break;
+    }
+    case 7: break;  // reference
+    case 8: {       // enumeration: base type, names, values
+        const int n = (int)(bits & 0xffff);
+        Type base;
+        if (!parse_type(c, base, depth + 1)) return false;
+        for (int m = 0; m < n && c.ok; m++) c.str(ver < 3);
+        c.skip((size_t)n * base.size);
+        break;
+    }
+    case 9: {  // variable length: base type
+        Type base;
+        if (!parse_type(c, base, depth + 1)) return false;
+        break;
+    }
+    case 10: {  // array
+        int rank = (int)c.u(1);
+        if (ver < 3) c.skip(3);
+        c.skip(4 * (size_t)rank);
+        if (ver < 3) c.skip(4 * (size_t)rank);
+        Type base;
+        if (!parse_type(c, base, depth + 1)) return false;
+        break;
+    }
+    default: return false;
+    }
+    return c.ok;
+}
+
+// A datatype's encoding in the earliest format (version 1).
+void encode_atomic(std::vector<uint8_t>& o, const Atomic& a)
+{
+    auto put = [&](uint64_t v, int n) {
+        for (int i = 0; i < n; i++) o.push_back((uint8_t)(v >> (8 * i)));
+    };
+    if (a.cls == 1) {
+        o.push_back(0x11);
+        o.push_back((uint8_t)((a.big_endian ? 1 : 0) | 0x20));  // mantissa normalisation: implied
+        o.push_back((uint8_t)(a.size == 8 ? 63 : 31));         // sign bit
+        o.push_back(0);
+        put(a.size, 4);
+        put(0, 2);
+        put(8 * a.size, 2);
+        if (a.size == 8) {
+            o.push_back(52); o.push_back(11); o.push_back(0); o.push_back(52); put(1023, 4);
+        } else {
+            o.push_back(23); o.push_back(8); o.push_back(0); o.push_back(23); put(127, 4);
+        }
+    } else {
+        o.push_back(0x10);
+        o.push_back((uint8_t)((a.big_endian ? 1 : 0) | (a.is_signed ? 8 : 0)));
+        o.push_back(0);
+        o.push_back(0);
+        put(a.size, 4);
+        put(0, 2);
+        put(8 * a.size, 2);
+    }
+}
+
+void encode_type(std::vector<uint8_t>& o, const Type& t)
+{
+    if (t.cls != 6) {
+        encode_atomic(o, t.atom);
+        return;
+    }
+    auto put = [&](uint64_t v, int n) {
+        for (int i = 0; i < n; i++) o.push_back((uint8_t)(v >> (8 * i)));
+    };
+    o.push_back(0x16);
+    put(t.members.size(), 3);
+    put(t.size, 4);
+    for (const Member& m : t.members) {
+        size_t n0 = o.size();
+        o.insert(o.end(), m.name.begin(), m.name.end());
+        o.push_back(0);
+        while ((o.size() - n0) % 8) o.push_back(0);
+        put(m.offset, 4);
+        put(0, 1);       // dimensionality
+        put(0, 3);       // reserved
+        put(0, 4);       // dimension permutation
+        put(0, 4);       // reserved
+        put(0, 16);      // dimension sizes
+        encode_atomic(o, m.type);
+    }
+}
+
+}  // namespace
+
+Type Type::ieee(int bytes, bool big_endian)
+{
+    Type t;
+    t.cls = 1;
+    t.size = (uint32_t)bytes;
+    t.atom = Atomic{1, (uint32_t)bytes, big_endian, true};
+    return t;
+}
+
+Type Type::compound_f64(const std::vector<std::string>& names, bool big_endian)
+{
+    Type t;
+    t.cls = 6;
+    t.size = (uint32_t)(8 * names.size());
+    for (size_t i = 0; i < names.size(); i++) t.members.push_back(Member{names[i], (uint32_t)(8 * i), {1, 8, big_endian, true}});
+    return t;
+}
+
+uint64_t Dataset::elements() const
+{
+    uint64_t n = 1;
+    for (uint64_t d : dims) n *= d;
+    return n;
+}
+
+double decode(const Atomic& t, const uint8_t* p)
+{
+    uint64_t v = 0;
+    if (t.big_endian)
+        for (uint32_t i = 0; i < t.size; i++) v = (v << 8) | p[i];
+    else
+        v = le(p, (int)t.size);
+    if (t.cls == 1) {
+        if (t.size == 4) {
+            uint32_t w = (uint32_t)v;
+            float f;
+            memcpy(&f, &w, 4);
+            return (double)f;
+        }
+        double d;
+        memcpy(&d, &v, 8);
+        return d;
+    }
+    if (t.is_signed && t.size < 8) {
+        const uint64_t sign = 1ull << (8 * t.size - 1);
+        if (v & sign) return (double)(int64_t)(v | ~((sign << 1) - 1));
+    }
+    return t.is_signed ? (double)(int64_t)v : (double)v;
+}
+
+bool raw_to_double(const Type& t, const uint8_t* raw, size_t n, double* out)
+{
+    if (t.cls != 0 && t.cls != 1) return false;
+    for (size_t i = 0; i < n; i++) out[i] = decode(t.atom, raw + i * t.size);
+    return true;
+}
+
+bool raw_to_float(const Type& t, const uint8_t* raw, size_t n, float* out)
+{
+    if (t.cls != 0 && t.cls != 1) return false;
+    for (size_t i = 0; i < n; i++) out[i] = (float)decode(t.atom, raw + i * t.size);
+    return true;
+}
+
+void put_f64(uint8_t* p, double v, bool big_endian)
+{
+    uint64_t w;
+    memcpy(&w, &v, 8);
+    for (int i = 0; i < 8; i++) p[big_endian ? 7 - i : i] = (uint8_t)(w >> (8 * i));
+}
+
+// ---------------------------------------------------------------- reader
+
+File::~File()
+{
+    if (fd_ >= 0) close(fd_);
+}
+
+bool File::fail(const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    err_ = path_ + ": " + buf;
+    return false;
+}
+
+bool File::rd(uint64_t addr, void* dst, size_t n)
+{
+    if (addr == kUndef || addr + base_ < addr || addr + base_ > size_ || n > size_ - (addr + base_))
+        return fail("read of %zu bytes at address %llu beyond the end of the file", n, (unsigned long long)addr);
+    uint8_t* d = (uint8_t*)dst;
+    uint64_t at = addr + base_;
+    while (n) {
+        ssize_t r = pread(fd_, d, n, (off_t)at);
+        if (r <= 0) {
+            if (r < 0 && errno == EINTR) continue;
+            return fail("read error at %llu", (unsigned long long)at);
+        }
+        d += r;
+        at += (uint64_t)r;
+        n -= (size_t)r;
+    }
+    return true;
+}
+
+bool File::open(const char* path)
+{
+    path_ = path ? path : "";
+    fd_ = ::open(path_.c_str(), O_RDONLY);
+    if (fd_ < 0) return fail("cannot open the file");
+    off_t end = lseek(fd_, 0, SEEK_END);
+    if (end < 0) return fail("cannot size the file");
+    size_ = (uint64_t)end;
+    static const uint8_t sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
+    uint64_t at = 0;
+    uint8_t sb[128];
+    for (;;) {  // the superblock sits at 0, 512, 1024, 2048, ... (after a user block)
+        if (at + 8 > size_) return fail("no HDF5 superblock found");
+        base_ = 0;
+        if (!rd(at, sb, 8)) return false;
+        if (!memcmp(sb, sig, 8)) break;
+        at = at ? 2 * at : 512;
+    }
+    const size_t avail = (size_t)std::min<uint64_t>(sizeof(sb), size_ - at);
+    if (!rd(at, sb, avail)) return false;
+    const int ver = sb[8];
+    if (ver > 1)
+        return fail("superblock version %d (the newer file format, libver 'latest'): not supported", ver);
+    if (sb[13] != 8 || sb[14] != 8) return fail("offsets of %d and lengths of %d bytes: not supported", sb[13], sb[14]);
+    size_t p = 24 + (ver == 1 ? 4 : 0);
+    if (avail < p + 32 + 40) return fail("truncated superblock");
+    base_ = le(sb + p, 8);
+    // root group symbol table entry: link name offset, object header address
+    root_ = le(sb + p + 32 + 8, 8);
+    if (base_ > size_) return fail("bad base address");
+    return true;
+}
+
+bool File::messages(uint64_t oh, std::vector<Msg>& out)
+{
+    out.clear();
+    uint8_t pre[16];
+    if (!rd(oh, pre, 16)) return false;
+    if (pre[0] != 1) {
+        if (!memcmp(pre, "OHDR", 4)) return fail("version 2 object header (the newer file format): not supported");
+        return fail("bad object header at %llu", (unsigned long long)oh);
+    }
+    const uint32_t nmsg = (uint32_t)le(pre + 2, 2);
+    std::vector<std::pair<uint64_t, uint64_t>> blocks{{oh + 16, le(pre + 8, 4)}};
+    uint32_t seen = 0;
+    for (size_t b = 0; b < blocks.size() && seen < nmsg; b++) {
+        if (blocks.size() > 4096 || blocks[b].second > (1ull << 30)) return fail("bad object header chunk");
+        std::vector<uint8_t> buf(blocks[b].second);
+        if (!rd(blocks[b].first, buf.data(), buf.size())) return false;
+        size_t q = 0;
+        while (q + 8 <= buf.size() && seen < nmsg) {
+            Msg m;
+            m.type = (uint16_t)le(&buf[q], 2);
+            const size_t sz = (size_t)le(&buf[q + 2], 2);
+            m.flags = buf[q + 4];
+            if (q + 8 + sz > buf.size()) return fail("object header message overruns its chunk");
+            m.data.assign(buf.begin() + q + 8, buf.begin() + q + 8 + sz);
+            q += 8 + sz;
+            seen++;
+            if (m.type == 0x10) {  // continuation: address, length
+                if (m.data.size() < 16) return fail("bad continuation message");
+                blocks.push_back({le(&m.data[0], 8), le(&m.data[8], 8)});
+            }
+            out.push_back(std::move(m));
+        }
+    }
+    return true;
+}
+
+bool File::btree_entries(uint64_t node, uint64_t heap_data, uint64_t heap_size, const std::string& name,
+                         uint64_t& oh, int depth)
+{
+    if (depth > 32) return fail("group B-tree too deep");
+    uint8_t h[24];
+    if (!rd(node, h, 24)) return false;
+    if (memcmp(h, "TREE", 4) || h[4] != 0) return fail("bad group B-tree node at %llu", (unsigned long long)node);
+    const int level = h[5], used = (int)le(h + 6, 2);
+    std::vector<uint8_t> kc((size_t)used * 16 + 8);
+    if (!rd(node + 24, kc.data(), kc.size())) return false;
+    for (int i = 0; i < used; i++) {
+        const uint64_t child = le(&kc[8 + 16 * (size_t)i], 8);
+        if (level > 0) {
+            if (!btree_entries(child, heap_data, heap_size, name, oh, depth + 1)) return false;
+            if (oh != kUndef) return true;
+            continue;
+        }
+        uint8_t sh[8];
+        if (!rd(child, sh, 8)) return false;
+        if (memcmp(sh, "SNOD", 4)) return fail("bad symbol table node at %llu", (unsigned long long)child);
+        const int nsym = (int)le(sh + 6, 2);
+        std::vector<uint8_t> ent((size_t)nsym * 40);
+        if (!rd(child + 8, ent.data(), ent.size())) return false;
+        for (int e = 0; e < nsym; e++) {
+            const uint64_t off = le(&ent[40 * (size_t)e], 8);
+            if (off >= heap_size) return fail("symbol name outside the local heap");
+            const size_t maxlen = (size_t)std::min<uint64_t>(heap_size - off, name.size() + 1);
+            std::vector<char> nm(maxlen);
+            if (!rd(heap_data + off, nm.data(), maxlen)) return false;
+            if (maxlen == name.size() + 1 && !memcmp(nm.data(), name.c_str(), maxlen)) {
+                oh = le(&ent[40 * (size_t)e + 8], 8);
+                return true;
+            }
+        }
+    }
+    return true;
+}
+
+bool File::group_entry(uint64_t group_oh, const std::string& name, uint64_t& oh)
+{
+    std::vector<Msg> ms;
+    if (!messages(group_oh, ms)) return false;
+    for (const Msg& m : ms) {
+        if (m.type == 0x06 || m.type == 0x02) return fail("group with link messages (the newer file format): not supported");
+        if (m.type != 0x11) continue;
+        if (m.data.size() < 16) return fail("bad symbol table message");
+        const uint64_t bt = le(&m.data[0], 8), hp = le(&m.data[8], 8);
+        uint8_t hh[32];
+        if (!rd(hp, hh, 32)) return false;
+        if (memcmp(hh, "HEAP", 4)) return fail("bad local heap at %llu", (unsigned long long)hp);
+        oh = kUndef;
+        if (!btree_entries(bt, le(hh + 24, 8), le(hh + 8, 8), name, oh, 0)) return false;
+        if (oh == kUndef) return fail("no object named '%s'", name.c_str());
+        return true;
+    }
+    return fail("object at %llu is not a group", (unsigned long long)group_oh);
+}
+
+bool File::dataset(const char* group, const char* name, Dataset& ds)
+{
+    if (fd_ < 0) return fail("file not open");
+    std::string path = std::string(group ? group : "") + "/" + (name ? name : "");
+    uint64_t oh = root_;
+    size_t i = 0;
+    while (i < path.size()) {
+        size_t j = path.find('/', i);
+        if (j == std::string::npos) j = path.size();
+        if (j > i && !group_entry(oh, path.substr(i, j - i), oh)) return false;
+        i = j + 1;
+    }
+    std::vector<Msg> ms;
+    if (!messages(oh, ms)) return false;
+    ds = Dataset();
+    bool have_space = false, have_type = false;
+    std::vector<uint8_t> fill;
+    for (const Msg& m : ms) {
+        Cur c{m.data.data(), m.data.data() + m.data.size()};
+        const bool shared = (m.flags & 2) != 0;
+        switch (m.type) {
+        case 0x01: {  // dataspace
+            if (shared) return fail("shared dataspace: not supported");
+            const int ver = (int)c.u(1), rank = (int)c.u(1), flags = (int)c.u(1);
+            if (ver == 1) {
+                c.skip(5);
+            } else if (ver == 2) {
+                if (c.u(1) == 2) return fail("null dataspace");
+            } else {
+                return fail("dataspace message version %d", ver);
+            }
+            for (int d = 0; d < rank; d++) ds.dims.push_back(c.u(8));
+            (void)flags;
+            if (!c.ok) return fail("bad dataspace message");
+            have_space = true;
+            break;
+        }
+        case 0x03:  // datatype
+            if (shared) return fail("shared (committed) datatype: not supported");
+            if (!parse_type(c, ds.type)) return fail("bad datatype message");
+            have_type = true;
+            break;
+        case 0x05: {  // fill value
+            const int ver = (int)c.u(1);
+            if (ver == 1 || ver == 2) {
+                c.skip(2);
+                const int defined = (int)c.u(1);
+                if (ver == 1 || defined) {
+                    const uint32_t sz = (uint32_t)c.u(4);
+                    if (c.need(sz)) fill.assign(c.p, c.p + sz);
+                }
+            } else if (ver == 3) {
+                const int flags = (int)c.u(1);
+                if (flags & 0x20) {
+                    const uint32_t sz = (uint32_t)c.u(4);
+                    if (c.need(sz)) fill.assign(c.p, c.p + sz);
+                }
+            }
+            break;
+        }
+        case 0x0b: {  // filter pipeline
+            const int ver = (int)c.u(1), n = (int)c.u(1);
+            if ((ver == 1 || ver == 2) && n > 0) ds.filtered = true;
+            break;
+        }
+        case 0x08: {  // data layout
+            const int ver = (int)c.u(1);
+            if (ver == 1 || ver == 2) {
+                const int dimensionality = (int)c.u(1), cls = (int)c.u(1);
+                c.skip(5);
+                if (cls != 0) ds.addr = c.u(8);
+                std::vector<uint64_t> ld;
+                for (int d = 0; d < dimensionality; d++) ld.push_back(c.u(4));
+                ds.layout = cls;
+                if (cls == 2 && dimensionality > 0) ds.chunk.assign(ld.begin(), ld.end() - 1);
+                if (cls == 0) {
+                    const uint32_t sz = (uint32_t)c.u(4);
+                    if (c.need(sz)) ds.compact.assign(c.p, c.p + sz);
+                }
+            } else if (ver == 3 || ver == 4) {
+                const int cls = (int)c.u(1);
+                ds.layout = cls;
+                if (cls == 0) {
+                    const uint32_t sz = (uint32_t)c.u(2);
+                    if (c.need(sz)) ds.compact.assign(c.p, c.p + sz);
+                } else if (cls == 1) {
+                    ds.addr = c.u(8);
+                    ds.bytes = c.u(8);
+                } else if (cls == 2 && ver == 3) {
+                    const int dimensionality = (int)c.u(1);
+                    ds.addr = c.u(8);
+                    for (int d = 0; d + 1 < dimensionality; d++) ds.chunk.push_back(c.u(4));
+                    c.skip(4);
+                } else {
+                    return fail("layout version %d class %d (the newer file format): not supported", ver, cls);
+                }
+            } else {
+                return fail("layout message version %d", ver);
+            }
+            if (!c.ok) return fail("bad layout message");
+            break;
+        }
+        default: break;
+        }
+    }
+    if (!have_space || !have_type || ds.layout < 0) return fail("'%s' is not a dataset", path.c_str());
+    if (ds.layout == 2 && ds.chunk.size() != ds.dims.size()) return fail("chunk rank differs from the dataspace's");
+    if (ds.layout == 1 && ds.bytes == 0 && ds.addr != kUndef) ds.bytes = ds.elements() * ds.type.size;
+    if (fill.size() == ds.type.size) ds.fill = fill;
+    return true;
+}
+
+bool File::chunk_index(const Dataset& ds, uint64_t node, int depth, std::vector<uint64_t>& keys,
+                       std::vector<uint64_t>& addrs, std::vector<uint32_t>& sizes)
+{
+    if (depth > 32) return fail("chunk B-tree too deep");
+    uint8_t h[24];
+    if (!rd(node, h, 24)) return false;
+    if (memcmp(h, "TREE", 4) || h[4] != 1) return fail("bad chunk B-tree node at %llu", (unsigned long long)node);
+    const int level = h[5], used = (int)le(h + 6, 2);
+    const size_t rank1 = ds.dims.size() + 1, ksz = 8 + 8 * rank1;
+    std::vector<uint8_t> kc((size_t)used * (ksz + 8) + ksz);
+    if (!rd(node + 24, kc.data(), kc.size())) return false;
+    for (int i = 0; i < used; i++) {
+        const uint8_t* k = &kc[(size_t)i * (ksz + 8)];
+        const uint64_t child = le(k + ksz, 8);
+        if (level > 0) {
+            if (!chunk_index(ds, child, depth + 1, keys, addrs, sizes)) return false;
+            continue;
+        }
+        if (le(k + 4, 4) != 0) return fail("filtered chunk: not supported");
+        for (size_t d = 0; d < ds.dims.size(); d++) keys.push_back(le(k + 8 + 8 * d, 8));
+        addrs.push_back(child);
+        sizes.push_back((uint32_t)le(k, 4));
+    }
+    return true;
+}
+
+bool File::read(const Dataset& ds, const uint64_t* offset, const uint64_t* count, void* raw)
+{
+    const size_t r = ds.dims.size(), es = ds.type.size;
+    uint64_t total = 1;
+    for (size_t d = 0; d < r; d++) {
+        if (offset[d] > ds.dims[d] || count[d] > ds.dims[d] - offset[d])
+            return fail("selection beyond the dataset's extent in dimension %zu", d);
+        total *= count[d];
+    }
+    uint8_t* out = (uint8_t*)raw;
+    if (total == 0) return true;
+    if (ds.filtered) return fail("compressed or filtered dataset: not supported");
+    // elements in dimensions d.. of the dataset and of the selection (the
+    // stride of dimension d is entry d + 1)
+    std::vector<uint64_t> dstride(r + 1, 1), sstride(r + 1, 1);
+    for (size_t d = r; d-- > 0;) {
+        dstride[d] = dstride[d + 1] * ds.dims[d];
+        sstride[d] = sstride[d + 1] * count[d];
+    }
+    if (ds.layout == 0 || ds.layout == 1) {
+        if (ds.layout == 1 && ds.addr == kUndef) {  // never written: fill value
+            for (uint64_t i = 0; i < total; i++)
+                if (!ds.fill.empty()) memcpy(out + i * es, ds.fill.data(), es);
+                else memset(out + i * es, 0, es);
+            return true;
+        }
+        if (r == 0) {  // scalar
+            if (ds.layout == 1) return rd(ds.addr, out, es);
+            if (ds.compact.size() < es) return fail("short compact data");
+            memcpy(out, ds.compact.data(), es);
+            return true;
+        }
+        if (ds.layout == 0 && ds.compact.size() < ds.elements() * es) return fail("short compact data");
+        // the longest run: trailing dimensions selected whole
+        size_t k = r - 1;
+        while (k > 0 && offset[k] == 0 && count[k] == ds.dims[k]) k--;
+        const uint64_t run = count[k] * dstride[k + 1];
+        const uint64_t nruns = total / run;
+        std::vector<uint64_t> idx(k + 1, 0);
+        for (uint64_t q = 0; q < nruns; q++) {
+            uint64_t lin = 0;
+            for (size_t d = 0; d <= k; d++) lin += (offset[d] + idx[d]) * dstride[d + 1];
+            if (ds.layout == 1) {
+                if (!rd(ds.addr + lin * es, out + q * run * es, run * es)) return false;
+            } else {
+                memcpy(out + q * run * es, ds.compact.data() + lin * es, run * es);
+            }
+            for (size_t d = k; d-- > 0;) {  // next index over dimensions 0..k-1
+                if (++idx[d] < count[d]) break;
+                idx[d] = 0;
+            }
+        }
+        return true;
+    }
+    // chunked: every stored chunk that meets the selection
+    std::vector<uint64_t> keys, addrs;
+    std::vector<uint32_t> sizes;
+    if (ds.addr != kUndef && !chunk_index(ds, ds.addr, 0, keys, addrs, sizes)) return false;
+    std::map<std::vector<uint64_t>, size_t> where;
+    for (size_t c = 0; c < addrs.size(); c++) where[std::vector<uint64_t>(keys.begin() + c * r, keys.begin() + (c + 1) * r)] = c;
+    uint64_t celems = 1;
+    for (size_t d = 0; d < r; d++) {
+        if (ds.chunk[d] == 0) return fail("zero chunk extent");
+        celems *= ds.chunk[d];
+    }
+    std::vector<uint8_t> cbuf(celems * es);
+    std::vector<uint64_t> first(r), last(r), ci(r);
+    for (size_t d = 0; d < r; d++) {
+        first[d] = offset[d] / ds.chunk[d];
+        last[d] = (offset[d] + count[d] - 1) / ds.chunk[d];
+        ci[d] = first[d];
+    }
+    for (;;) {
+        std::vector<uint64_t> origin(r);
+        for (size_t d = 0; d < r; d++) origin[d] = ci[d] * ds.chunk[d];
+        auto it = where.find(origin);
+        if (it == where.end()) {
+            for (uint64_t i = 0; i < celems; i++)
+                if (!ds.fill.empty()) memcpy(&cbuf[i * es], ds.fill.data(), es);
+                else memset(&cbuf[i * es], 0, es);
+        } else {
+            if (sizes[it->second] < cbuf.size()) return fail("short chunk");
+            if (!rd(addrs[it->second], cbuf.data(), cbuf.size())) return false;
+        }
+        // copy the part of this chunk inside the selection, element rows of the last dimension
+        std::vector<uint64_t> lo(r), hi(r);
+        for (size_t d = 0; d < r; d++) {
+            lo[d] = std::max(origin[d], offset[d]);
+            hi[d] = std::min(origin[d] + ds.chunk[d], offset[d] + count[d]);
+        }
+        std::vector<uint64_t> p(lo);
+        const uint64_t rowlen = hi[r - 1] - lo[r - 1];
+        for (;;) {
+            uint64_t src = 0, dst = 0, cstride = 1;
+            for (size_t d = r; d-- > 0;) {
+                src += (p[d] - origin[d]) * cstride;
+                cstride *= ds.chunk[d];
+                dst += (p[d] - offset[d]) * sstride[d + 1];
+            }
+            memcpy(out + dst * es, &cbuf[src * es], rowlen * es);
+            size_t d = r - 1;
+            bool more = false;
+            while (d-- > 0) {
+                if (++p[d] < hi[d]) {
+                    more = true;
+                    break;
+                }
+                p[d] = lo[d];
+            }
+            if (!more) break;
+        }
+        size_t d = r;
+        bool more = false;
+        while (d-- > 0) {
+            if (++ci[d] <= last[d]) {
+                more = true;
+                break;
+            }
+            ci[d] = first[d];
+        }
+        if (!more) break;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------- writer
+
+namespace {
+
+struct Buf {
+    std::vector<uint8_t>& v;
+    void at(uint64_t a)
+    {
+        if (v.size() < a) v.resize(a, 0);
+    }
+    void put(uint64_t a, uint64_t x, int n)
+    {
+        if (v.size() < a + n) v.resize(a + n, 0);
+        for (int i = 0; i < n; i++) v[a + i] = (uint8_t)(x >> (8 * i));
+    }
+    void bytes(uint64_t a, const void* p, size_t n)
+    {
+        if (v.size() < a + n) v.resize(a + n, 0);
+        memcpy(&v[a], p, n);
+    }
+};
+
+constexpr int kLeafK = 4, kInternalK = 16;
+constexpr uint64_t kSuper = 96;
+constexpr uint64_t kGroupOH = 16 + 8 + 16;
+constexpr uint64_t kTree = 24 + (2 * kInternalK + 1) * 8 + 2 * kInternalK * 8;
+constexpr uint64_t kHeapHdr = 32;
+constexpr uint64_t kSnod = 8 + 2 * kLeafK * 40;
+
+struct GroupAt {
+    uint64_t oh, tree, heap, heap_data, heap_size, snod;
+    int nsnod;
+    std::vector<std::pair<std::string, uint64_t>> names;  // sorted; heap offset
+};
+
+}  // namespace
+
+const WDataset* Plan::find(const std::string& group, const std::string& name) const
+{
+    for (const WGroup& g : groups)
+        if (g.name == group)
+            for (const WDataset& d : g.dsets)
+                if (d.name == name) return &d;
+    return nullptr;
+}
+
+bool Plan::plan()
+{
+    meta.clear();
+    err.clear();
+    // the symbols of every group: the root's children, then each child's datasets
+    std::vector<std::vector<std::string>> syms(groups.size() + 1);
+    for (const WGroup& g : groups) {
+        if (g.name.empty()) {
+            for (const WDataset& d : g.dsets) syms[0].push_back(d.name);
+        } else {
+            if (g.name.find('/') != std::string::npos) {
+                err = "nested group names are not supported";
+                return false;
+            }
+            syms[0].push_back(g.name);
+        }
+    }
+    for (size_t i = 0; i < groups.size(); i++)
+        if (!groups[i].name.empty())
+            for (const WDataset& d : groups[i].dsets) syms[i + 1].push_back(d.name);
+    for (auto& s : syms) {
+        std::sort(s.begin(), s.end());
+        if (std::adjacent_find(s.begin(), s.end()) != s.end()) {
+            err = "duplicate name in a group";
+            return false;
+        }
+        if (s.size() > (size_t)2 * kInternalK * 2 * kLeafK) {
+            err = "too many objects in one group";
+            return false;
+        }
+        for (const std::string& n : s)
+            if (n.empty() || n.find('/') != std::string::npos) {
+                err = "bad object name";
+                return false;
+            }
+    }
+    // addresses of the group structures
+    uint64_t a = kSuper;
+    std::vector<GroupAt> ga(syms.size());
+    for (size_t i = 0; i < syms.size(); i++) {
+        if (i > 0 && groups[i - 1].name.empty()) continue;
+        GroupAt& g = ga[i];
+        uint64_t off = 8;  // offset 0 holds the empty string
+        for (const std::string& n : syms[i]) {
+            g.names.push_back({n, off});
+            off += pad8(n.size() + 1);
+        }
+        g.heap_size = off + 16;  // one free block at the end
+        g.nsnod = (int)((syms[i].size() + 2 * kLeafK - 1) / (2 * kLeafK));
+        g.oh = a; a += kGroupOH;
+        g.tree = a; a += kTree;
+        g.heap = a; a += kHeapHdr;
+        g.heap_data = a; a += g.heap_size;
+        g.snod = a; a += kSnod * (uint64_t)g.nsnod;
+    }
+    // dataset object headers
+    std::vector<std::vector<uint8_t>> dtypes;
+    std::map<std::string, uint64_t> oh_of;  // "group/name" -> object header
+    std::vector<WDataset*> order;
+    for (WGroup& g : groups)
+        for (WDataset& d : g.dsets) {
+            std::vector<uint8_t> t;
+            encode_type(t, d.type);
+            const uint64_t ohsz = 16 + (8 + 8 + 8 * d.dims.size()) + (8 + pad8(t.size())) + (8 + 8) + (8 + 24);
+            oh_of[g.name + "/" + d.name] = a;
+            a += ohsz;
+            dtypes.push_back(t);
+            order.push_back(&d);
+        }
+    const uint64_t meta_end = a;
+    for (WDataset* d : order) {
+        uint64_t n = 1;
+        for (uint64_t x : d->dims) n *= x;
+        d->bytes = n * d->type.size;
+        if (d->bytes == 0) {
+            d->addr = kUndef;
+            continue;
+        }
+        a = (a + 15) & ~15ull;
+        d->addr = a;
+        a += d->bytes;
+    }
+    eof = a;
+    Buf b{meta};
+    // superblock version 0
+    static const uint8_t sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
+    b.bytes(0, sig, 8);
+    b.put(8, 0, 1); b.put(9, 0, 1); b.put(10, 0, 1); b.put(11, 0, 1); b.put(12, 0, 1);
+    b.put(13, 8, 1); b.put(14, 8, 1); b.put(15, 0, 1);
+    b.put(16, kLeafK, 2); b.put(18, kInternalK, 2); b.put(20, 0, 4);
+    b.put(24, 0, 8);       // base address
+    b.put(32, kUndef, 8);  // free-space info
+    b.put(40, eof, 8);     // end of file
+    b.put(48, kUndef, 8);  // driver info
+    b.put(56, 0, 8); b.put(64, ga[0].oh, 8); b.put(72, 1, 4); b.put(76, 0, 4);
+    b.put(80, ga[0].tree, 8); b.put(88, ga[0].heap, 8);
+    for (size_t i = 0; i < syms.size(); i++) {
+        if (i > 0 && groups[i - 1].name.empty()) continue;
+        const GroupAt& g = ga[i];
+        // object header: one symbol table message
+        b.put(g.oh, 1, 1); b.put(g.oh + 1, 0, 1); b.put(g.oh + 2, 1, 2); b.put(g.oh + 4, 1, 4); b.put(g.oh + 8, 24, 4);
+        b.put(g.oh + 16, 0x11, 2); b.put(g.oh + 18, 16, 2); b.put(g.oh + 20, 1, 1);
+        b.put(g.oh + 24, g.tree, 8); b.put(g.oh + 32, g.heap, 8);
+        // B-tree node (type 0, leaf level) with one child per symbol table node
+        b.bytes(g.tree, "TREE", 4); b.put(g.tree + 4, 0, 1); b.put(g.tree + 5, 0, 1);
+        b.put(g.tree + 6, (uint64_t)g.nsnod, 2); b.put(g.tree + 8, kUndef, 8); b.put(g.tree + 16, kUndef, 8);
+        b.put(g.tree + 24, 0, 8);
+        for (int s = 0; s < g.nsnod; s++) {
+            const size_t lastsym = std::min(g.names.size(), (size_t)(s + 1) * 2 * kLeafK) - 1;
+            b.put(g.tree + 32 + 16 * (uint64_t)s, g.snod + kSnod * (uint64_t)s, 8);
+            b.put(g.tree + 40 + 16 * (uint64_t)s, g.names[lastsym].second, 8);
+        }
+        b.at(g.tree + kTree);
+        // local heap: the names, then a free block (next: 1 = none, size)
+        b.bytes(g.heap, "HEAP", 4); b.put(g.heap + 4, 0, 4);
+        b.put(g.heap + 8, g.heap_size, 8); b.put(g.heap + 16, g.heap_size - 16, 8); b.put(g.heap + 24, g.heap_data, 8);
+        b.put(g.heap_data, 0, 8);
+        for (const auto& nm : g.names) b.bytes(g.heap_data + nm.second, nm.first.c_str(), nm.first.size() + 1);
+        b.put(g.heap_data + g.heap_size - 16, 1, 8);
+        b.put(g.heap_data + g.heap_size - 8, 16, 8);
+        // symbol table nodes
+        for (int s = 0; s < g.nsnod; s++) {
+            const uint64_t sn = g.snod + kSnod * (uint64_t)s;
+            const size_t e0 = (size_t)s * 2 * kLeafK, e1 = std::min(g.names.size(), e0 + 2 * kLeafK);
+            b.bytes(sn, "SNOD", 4); b.put(sn + 4, 1, 1); b.put(sn + 5, 0, 1); b.put(sn + 6, e1 - e0, 2);
+            for (size_t e = e0; e < e1; e++) {
+                const uint64_t en = sn + 8 + 40 * (uint64_t)(e - e0);
+                const std::string& nm = g.names[e].first;
+                b.put(en, g.names[e].second, 8);
+                if (i == 0) {
+                    // a child group (cache type 1: its B-tree and heap) or a root dataset
+                    size_t gi = 0;
+                    for (; gi < groups.size(); gi++)
+                        if (groups[gi].name == nm) break;
+                    if (gi < groups.size()) {
+                        b.put(en + 8, ga[gi + 1].oh, 8); b.put(en + 16, 1, 4);
+                        b.put(en + 24, ga[gi + 1].tree, 8); b.put(en + 32, ga[gi + 1].heap, 8);
+                    } else {
+                        b.put(en + 8, oh_of["/" + nm], 8); b.put(en + 16, 0, 4);
+                    }
+                } else {
+                    b.put(en + 8, oh_of[groups[i - 1].name + "/" + nm], 8); b.put(en + 16, 0, 4);
+                }
+            }
+            b.at(sn + kSnod);
+        }
+    }
+    // dataset object headers: dataspace, datatype, fill value, layout
+    size_t k = 0;
+    for (WGroup& g : groups)
+        for (WDataset& d : g.dsets) {
+            const std::vector<uint8_t>& t = dtypes[k++];
+            uint64_t o = oh_of[g.name + "/" + d.name];
+            const uint64_t body = (8 + 8 + 8 * d.dims.size()) + (8 + pad8(t.size())) + (8 + 8) + (8 + 24);
+            b.put(o, 1, 1); b.put(o + 1, 0, 1); b.put(o + 2, 4, 2); b.put(o + 4, 1, 4); b.put(o + 8, body, 4);
+            uint64_t m = o + 16;
+            b.put(m, 0x01, 2); b.put(m + 2, 8 + 8 * d.dims.size(), 2); b.put(m + 4, 0, 1);
+            b.put(m + 8, 1, 1); b.put(m + 9, d.dims.size(), 1); b.put(m + 10, 0, 1);
+            for (size_t x = 0; x < d.dims.size(); x++) b.put(m + 16 + 8 * x, d.dims[x], 8);
+            m += 8 + 8 + 8 * d.dims.size();
+            b.put(m, 0x03, 2); b.put(m + 2, pad8(t.size()), 2); b.put(m + 4, 1, 1);
+            b.bytes(m + 8, t.data(), t.size());
+            m += 8 + pad8(t.size());
+            // fill value message version 1: allocation late, write if set, default value
+            b.put(m, 0x05, 2); b.put(m + 2, 8, 2); b.put(m + 4, 1, 1);
+            b.put(m + 8, 1, 1); b.put(m + 9, 2, 1); b.put(m + 10, 2, 1); b.put(m + 11, 1, 1); b.put(m + 12, 0, 4);
+            m += 16;
+            // layout message version 3: contiguous, address, size
+            b.put(m, 0x08, 2); b.put(m + 2, 24, 2); b.put(m + 4, 0, 1);
+            b.put(m + 8, 3, 1); b.put(m + 9, 1, 1); b.put(m + 10, d.addr, 8); b.put(m + 18, d.bytes, 8);
+            m += 32;
+        }
+    b.at(meta_end);
+    // zero padding up to the first data region
+    uint64_t first = eof;
+    for (WDataset* d : order)
+        if (d->addr != kUndef) first = std::min(first, d->addr);
+    b.at(first);
+    return true;
+}
+
+int open_for_write(const char* path, std::string& err)
+{
+    int fd = ::open(path, O_WRONLY | O_CREAT, 0644);
+    if (fd < 0) err = std::string(path) + ": cannot open for writing";
+    return fd;
+}
+
+static bool pwrite_all(int fd, const void* p, size_t n, uint64_t at)
+{
+    const uint8_t* s = (const uint8_t*)p;
+    while (n) {
+        ssize_t w = pwrite(fd, s, n, (off_t)at);
+        if (w <= 0) {
+            if (w < 0 && errno == EINTR) continue;
+            return false;
+        }
+        s += w;
+        at += (uint64_t)w;
+        n -= (size_t)w;
+    }
+    return true;
+}
+
+bool write_meta(int fd, const Plan& plan, std::string& err)
+{
+    if (!pwrite_all(fd, plan.meta.data(), plan.meta.size(), 0)) {
+        err = "write of the file's metadata failed";
+        return false;
+    }
+    // zero the gaps between data regions, then fix the length
+    std::vector<const WDataset*> ds;
+    for (const WGroup& g : plan.groups)
+        for (const WDataset& d : g.dsets)
+            if (d.addr != kUndef) ds.push_back(&d);
+    std::sort(ds.begin(), ds.end(), [](const WDataset* x, const WDataset* y) { return x->addr < y->addr; });
+    uint64_t at = plan.meta.size();
+    static const uint8_t zero[16] = {0};
+    for (const WDataset* d : ds) {
+        if (d->addr > at && !pwrite_all(fd, zero, (size_t)(d->addr - at), at)) {
+            err = "write failed";
+            return false;
+        }
+        at = d->addr + d->bytes;
+    }
+    if (ftruncate(fd, (off_t)plan.eof) != 0) {
+        err = "cannot set the file's length";
+        return false;
+    }
+    return true;
+}
+
+bool write_elements(int fd, const WDataset& d, uint64_t first, uint64_t n, const void* bytes, std::string& err)
+{
+    if (n == 0) return true;
+    if (d.addr == kUndef || (first + n) * d.type.size > d.bytes) {
+        err = "records beyond the dataset's extent";
+        return false;
+    }
+    if (!pwrite_all(fd, bytes, (size_t)(n * d.type.size), d.addr + first * d.type.size)) {
+        err = "write of the records failed";
+        return false;
+    }
+    return true;
+}
+
+}  // namespace tph5

@@ -1,5 +1,5 @@
-// loaders.cu -- PIC-style E and B read from the reference's binary field
-// files straight into device memory.
+// loaders.cu -- PIC-style E and B read from the reference's binary and HDF5
+// field files straight into device memory.
 //
 // The reference reads bx_<ct>.gda, by_, bz_ and ex_, ey_, ez_ (nx*ny*nz FP32
 // each, x fastest) into host arrays of {x,y,z} records scaled by B0 or E0
@@ -11,10 +11,13 @@
 // mixed path's interleaved grid and the single-point functions then use the
 // device copy, and the host arrays stay untouched (tp_fetch_device_fields
 // copies them back when a caller needs them).
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 
 #include "../../include/tp_gpu.h"
+#include "../../include/tp_h5.h"
+#include "h5lite.h"
 #include "tp_internal.h"
 
 using namespace tp;
@@ -73,6 +76,50 @@ bool read_component(const char* fname, size_t n, float* dcomp, Staging& st, cuda
     }
     fclose(fp);
     return ok;
+}
+
+// One raw HDF5 value (ES bytes, big-endian or not) as the float the
+// reference's H5Dread with a float memory type gives: doubles rounded to
+// nearest, as a C cast.
+template <int ES, bool BE>
+__device__ __forceinline__ float h5_value(const unsigned char* __restrict__ p)
+{
+    if (ES == 4) {
+        unsigned int w = *(const unsigned int*)p;
+        if (BE) w = __byte_perm(w, 0, 0x0123);
+        return __uint_as_float(w);
+    } else {
+        unsigned long long w = *(const unsigned long long*)p;
+        if (BE) {
+            const unsigned int lo = (unsigned int)w, hi = (unsigned int)(w >> 32);
+            w = ((unsigned long long)__byte_perm(lo, 0, 0x0123) << 32) | __byte_perm(hi, 0, 0x0123);
+        }
+        return (float)__longlong_as_double((long long)w);
+    }
+}
+
+// The reference's C-to-Fortran reorder (src/magnetic_field.c:656-665): the
+// value at [i][j][k] of the file's [nx][ny][nz] array goes to record
+// (k * ny + j) * nx + i, scaled.  32 x 32 tiles of (i, k) at one j through
+// shared memory, so that both the reads (along k) and the writes (along i)
+// are coalesced.  Block (32, 8); grid (ceil(nz / 32), ceil(nx / 32), ny).
+template <int ES, bool BE>
+__global__ void __launch_bounds__(256) h5_transpose_kernel(const unsigned char* __restrict__ raw, int nx,
+                                                          int ny, int nz, double scale, int k,
+                                                          float* __restrict__ rec)
+{
+    __shared__ float tile[32][33];
+    const int k0 = blockIdx.x * 32, i0 = blockIdx.y * 32, j = blockIdx.z;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int i = i0 + r, kk = k0 + threadIdx.x;
+        if (i < nx && kk < nz) tile[r][threadIdx.x] = h5_value<ES, BE>(raw + (((size_t)i * ny + j) * nz + kk) * ES);
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int kk = k0 + r, i = i0 + threadIdx.x;
+        if (i < nx && kk < nz)
+            rec[3 * (((size_t)kk * ny + j) * nx + i) + k] = (float)((double)tile[threadIdx.x][r] * scale);
+    }
 }
 
 bool device_records(Mirror& m, size_t bytes)
@@ -151,4 +198,100 @@ extern "C" int tp_fetch_device_fields(float* host_e, float* host_b)
     if (host_e) cudaMemcpyAsync(host_e, g.m_ec_f.dev, g.m_ec_f.bytes, cudaMemcpyDeviceToHost, s);
     if (host_b) cudaMemcpyAsync(host_b, g.m_bc_f.dev, g.m_bc_f.bytes, cudaMemcpyDeviceToHost, s);
     return cuda_ok(cudaStreamSynchronize(s), "fetch fields") ? 0 : -1;
+}
+
+// tp_read_pic_fields_h5: read_pic_bfields_float_h5 / read_pic_efields_float_h5
+// (src/magnetic_field.c:632-692, src/electric_field.c:447-507) into device
+// memory.  Each dataset's [0, nx) x [0, ny) x [0, nz) block streams from the
+// file in whole i-planes through two pinned buffers (reading the next piece
+// while the previous one copies), then one transpose kernel writes the
+// component into the records.
+extern "C" int tp_read_pic_fields_h5(const char* fname, const char* gname, int with_e)
+{
+    if (!ensure_init()) return -1;
+    if (multi_tframe != 0) {
+        set_error(7, "tp_read_pic_fields_h5 reads one time frame (multi_tframe 0)");
+        return -1;
+    }
+    const int nx = simul_grid.nx, ny = simul_grid.ny, nz = simul_grid.nz;
+    if (nx < 1 || ny < 1 || nz < 1 || ny > 65535 || (nx + 31) / 32 > 65535 || !fname) {
+        set_error(7, "tp_read_pic_fields_h5: grid %d x %d x %d or no file name", nx, ny, nz);
+        return -1;
+    }
+    const size_t n = (size_t)nx * ny * nz;
+    tph5::File f;
+    if (!f.open(fname)) {
+        set_error(7, "%s", f.error().c_str());
+        return -1;
+    }
+    const char* names[6] = {"cbx", "cby", "cbz", "ex", "ey", "ez"};
+    tph5::Dataset ds[6];
+    const int ncomp = with_e ? 6 : 3;
+    size_t es_max = 4;
+    for (int c = 0; c < ncomp; c++) {
+        if (!f.dataset(gname, names[c], ds[c])) {
+            set_error(7, "%s", f.error().c_str());
+            return -1;
+        }
+        const tph5::Dataset& d = ds[c];
+        if (d.dims.size() != 3 || d.dims[0] < (uint64_t)nx || d.dims[1] < (uint64_t)ny || d.dims[2] < (uint64_t)nz) {
+            set_error(7, "%s: dataset %s is not an array of at least %d x %d x %d", fname, names[c], nx, ny, nz);
+            return -1;
+        }
+        if (d.type.cls != 1) {
+            set_error(7, "%s: dataset %s is not floating point", fname, names[c]);
+            return -1;
+        }
+        if (d.type.size > es_max) es_max = d.type.size;
+    }
+    cudaStream_t s = g.stream;
+    static Scratch raw_dev;
+    unsigned char* draw = (unsigned char*)raw_dev.get(es_max * n);
+    if (!draw) return -1;
+    const size_t plane = (size_t)ny * nz;
+    Staging st;
+    const size_t piece_planes = std::max<size_t>(1, std::min<size_t>(nx, (sizeof(float) * kPiece) / (es_max * plane)));
+    for (int b = 0; b < 2; b++)
+        if (!cuda_ok(cudaMallocHost(&st.host[b], es_max * plane * piece_planes), "pinned staging") ||
+            !cuda_ok(cudaEventCreateWithFlags(&st.done[b], cudaEventDisableTiming), "staging event") ||
+            !cuda_ok(cudaEventRecord(st.done[b], s), "staging event"))
+            return -1;
+    if (!device_records(g.m_bc_f, sizeof(float) * 3 * n) || !device_records(g.m_ec_f, sizeof(float) * 3 * n))
+        return -1;
+    auto fail = [&]() {
+        g.m_bc_f.release();
+        g.m_ec_f.release();
+        return -1;
+    };
+    if (!with_e && !cuda_ok(cudaMemsetAsync(g.m_ec_f.dev, 0, sizeof(float) * 3 * n, s), "E records")) return fail();
+    for (int c = 0; c < ncomp; c++) {
+        const tph5::Dataset& d = ds[c];
+        const size_t es = d.type.size;
+        int b = 0;
+        for (size_t i0 = 0; i0 < (size_t)nx; i0 += piece_planes) {
+            const size_t m = std::min(piece_planes, (size_t)nx - i0);
+            if (!cuda_ok(cudaEventSynchronize(st.done[b]), "staging")) return fail();
+            const uint64_t off[3] = {i0, 0, 0}, cnt[3] = {m, (uint64_t)ny, (uint64_t)nz};
+            if (!f.read(d, off, cnt, st.host[b])) {
+                set_error(7, "%s", f.error().c_str());
+                return fail();
+            }
+            if (!cuda_ok(cudaMemcpyAsync(draw + i0 * plane * es, st.host[b], m * plane * es, cudaMemcpyHostToDevice, s),
+                         "field upload") ||
+                !cuda_ok(cudaEventRecord(st.done[b], s), "staging event"))
+                return fail();
+            b ^= 1;
+        }
+        float* rec = (float*)(c < 3 ? g.m_bc_f.dev : g.m_ec_f.dev);
+        const dim3 grid((unsigned)((nz + 31) / 32), (unsigned)((nx + 31) / 32), (unsigned)ny), block(32, 8);
+        const double scale = c < 3 ? B0 : E0;
+        const bool be = d.type.atom.big_endian;
+        if (es == 4 && !be) h5_transpose_kernel<4, false><<<grid, block, 0, s>>>(draw, nx, ny, nz, scale, c % 3, rec);
+        else if (es == 4) h5_transpose_kernel<4, true><<<grid, block, 0, s>>>(draw, nx, ny, nz, scale, c % 3, rec);
+        else if (!be) h5_transpose_kernel<8, false><<<grid, block, 0, s>>>(draw, nx, ny, nz, scale, c % 3, rec);
+        else h5_transpose_kernel<8, true><<<grid, block, 0, s>>>(draw, nx, ny, nz, scale, c % 3, rec);
+        if (!cuda_ok(cudaGetLastError(), "field transpose")) return fail();
+    }
+    g.upload_gen++;
+    return cuda_ok(cudaStreamSynchronize(s), "field read") ? 0 : fail();
 }

@@ -7,6 +7,7 @@
 #include <cstring>
 
 #include "../../include/tp_gpu.h"
+#include "../../include/tp_h5.h"
 #include "tp_internal.h"
 #include "tp_kernels.h"
 
@@ -73,32 +74,18 @@ extern "C" int tp_poincare_trace(int n, const double* seeds, int face, double st
 }
 
 // Default output of poincare_map when the caller provides none: the
-// reference writes /poincare_map/{xpos,ypos,zpos} [points][ncross + 1] to
-// data/poincare_map.h5 with parallel HDF5 (src/poincare_map.c:185-235); this
-// library does not link HDF5, so the default writes the same arrays as raw
-// doubles to data/poincare_map.bin (one process) or data/poincare_map.<rank>.bin,
-// after a header of four 32-bit integers: points in total, ncross + 1, this
-// rank's first point, this rank's points.  A caller with HDF5 defines this
-// function to keep the reference's file.
+// reference's data/poincare_map.h5 (src/poincare_map.c:185-235), group
+// /poincare_map, datasets xpos, ypos, zpos [points][ncross + 1] of native
+// doubles, each rank writing its rows (tp_h5_write_poincare, no libhdf5).  A
+// caller may define this function to write the points elsewhere.
 extern "C" __attribute__((weak)) void tp_poincare_save(int mpi_rank, int mpi_size, int npoints_total,
                                                        int nc, int nshift, int npoints, const double* xpos,
                                                        const double* ypos, const double* zpos)
 {
-    char name[256];
-    if (mpi_size > 1) snprintf(name, sizeof(name), "data/poincare_map.%d.bin", mpi_rank);
-    else snprintf(name, sizeof(name), "data/poincare_map.bin");
-    FILE* fp = fopen(name, "wb");
-    if (!fp) {
-        printf("ERROR: cannot write %s\n", name);
-        exit(1);
-    }
-    int hdr[4] = {npoints_total, nc + 1, nshift, npoints};
-    size_t m = (size_t)npoints * (nc + 1);
-    bool ok = fwrite(hdr, sizeof(int), 4, fp) == 4 && fwrite(xpos, sizeof(double), m, fp) == m &&
-              fwrite(ypos, sizeof(double), m, fp) == m && fwrite(zpos, sizeof(double), m, fp) == m;
-    fclose(fp);
-    if (!ok) {
-        printf("ERROR: short write to %s\n", name);
+    (void)mpi_rank;
+    (void)mpi_size;
+    if (tp_h5_write_poincare("data/poincare_map.h5", npoints_total, nc, nshift, npoints, xpos, ypos, zpos) != 0) {
+        printf("ERROR: %s\n", tp_last_error());
         exit(1);
     }
 }

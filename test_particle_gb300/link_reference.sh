@@ -1,7 +1,8 @@
 #!/usr/bin/env bash
 # Links the reference's own program (main.c and every module that is not on
 # the tracking hot path) against libtpgpu.so instead of tracking.o,
-# emfields.o, interpolation.o, force_free.o, wlcs.o and poincare_map.o.
+# emfields.o, interpolation.o, force_free.o, wlcs.o, poincare_map.o and
+# data_io.o (the field-file readers, HDF5 included, come from the library).
 #
 #   REF      reference tree (default: $TP_REFERENCE_DIR)
 #   CC       the reference's compiler (mpicc on a cluster)
@@ -26,7 +27,7 @@ LIBDIR="$HERE/_build"
 [ -f "$LIBDIR/libtpgpu.so" ] || { echo "build libtpgpu.so first" >&2; exit 2; }
 mkdir -p "$OUT/obj"
 FLAGS=(-O2 -fopenmp -fcommon -std=gnu99 -w -include stdbool.h -I"$REF/include" ${CFLAGS:-})
-KEEP=(main test_particle domain diagnostics particle_info data_io quick_sort bessel
+KEEP=(main test_particle domain diagnostics particle_info quick_sort bessel
       magnetic_field electric_field velocity_field)
 for s in "${KEEP[@]}"; do
   "$CC" "${FLAGS[@]}" -c "$REF/src/$s.c" -o "$OUT/obj/$s.o"

@@ -1,5 +1,5 @@
 """The reference's own program links against libtpgpu.so in place of its
-tracking, emfields, interpolation, force_free, wlcs and poincare_map objects
+tracking, emfields, interpolation, force_free, wlcs, poincare_map and data_io objects
 (test_particle_gb300/link_reference.sh).  Needs the reference tree (read only)
 and a compiler; linking needs no GPU."""
 import os
@@ -41,6 +41,8 @@ def test_reference_program_links_against_library(tmp_path):
     for name in ("particle_tracking_hybrid", "set_variables_tracking", "set_ptl_params_tracking",
                  "set_variables_emfields", "get_emf", "getemf_ff",
                  "getemf_wlcs", "get_trilinar_parameters", "get_param_ff", "read_wlcs",
-                 "free_config", "adjust_dt_normI", "get_tracking_time_interval", "poincare_map"):
+                 "free_config", "adjust_dt_normI", "get_tracking_time_interval", "poincare_map",
+                 "read_data_serial_float_h5", "read_data_serial_double_h5", "read_data_serial_float_binary",
+                 "read_data_serial_double_binary"):
         assert name in need, name
     assert need <= exported, sorted(need - exported)
