@@ -431,7 +431,10 @@ def write(path, tree, *, userblock=0, superblock=0, layout="contiguous", layout_
             o.put(sn, b"SNOD" + bytes([1, 0]) + struct.pack("<H", len(part)))
             for e, (name, oh, cache) in enumerate(part):
                 ent = struct.pack("<QQ", offs[s0 + e], oh)
-                ent += struct.pack("<II", 1, 0) + struct.pack("<QQ", *cache) if cache else struct.pack("<II", 0, 0) + b"\0" * 16
+                if cache:  # a group: cache type 1 with its B-tree and heap
+                    ent += struct.pack("<II", 1, 0) + struct.pack("<QQ", *cache)
+                else:
+                    ent += struct.pack("<II", 0, 0) + b"\0" * 16
                 o.put(sn + 8 + 40 * e, ent)
             snods.append((rel(sn), offs[s0 + len(part) - 1]))
         tree = o.alloc(24 + 33 * 8 + 32 * 8)

@@ -21,6 +21,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <vector>
 
 #include "../../include/tp_gpu.h"
@@ -46,6 +47,21 @@ tph5::Plan particles_plan(unsigned long long ntot)
     p.groups.push_back(g);
     p.plan();
     return p;
+}
+
+// A C entry point's body: exceptions (an allocation that failed for a
+// corrupted extent, say) become an error status, never cross the C ABI.
+template <class F>
+int guarded(const char* what, F body)
+{
+    try {
+        return body();
+    } catch (const std::exception& e) {
+        set_error(7, "%s: %s", what, e.what());
+    } catch (...) {
+        set_error(7, "%s failed", what);
+    }
+    return -1;
 }
 
 struct Fd {
@@ -83,6 +99,10 @@ bool h5_read_as(const char* fname, const char* gname, const char* dset, int rank
     for (int d = 0; d < rank; d++) {
         o[d] = offset[d];
         c[d] = count[d];
+        if (o[d] > ds.dims[d] || c[d] > ds.dims[d] - o[d]) {
+            set_error(7, "%s: selection beyond the dataset's extent in dimension %d", fname, d);
+            return false;
+        }
         n *= c[d];
     }
     std::vector<uint8_t> raw(n * ds.type.size);
@@ -97,14 +117,14 @@ bool h5_read_as(const char* fname, const char* gname, const char* dset, int rank
 
 }  // namespace
 
-extern "C" int tp_h5_read(const char* fname, const char* gname, const char* dset, int rank,
+static int tp_h5_read_impl(const char* fname, const char* gname, const char* dset, int rank,
                           const unsigned long long* count, const unsigned long long* offset, int elem_bytes,
                           void* data)
 {
     return h5_read_as(fname, gname, dset, rank, count, offset, elem_bytes, data) ? 0 : -1;
 }
 
-extern "C" int tp_h5_info(const char* fname, const char* gname, const char* dset, int* rank,
+static int tp_h5_info_impl(const char* fname, const char* gname, const char* dset, int* rank,
                           unsigned long long* dims, int* type_class, int* type_size)
 {
     tph5::File f;
@@ -130,13 +150,17 @@ extern "C" int tp_h5_info(const char* fname, const char* gname, const char* dset
 extern "C" void read_data_serial_double_h5(int rank, unsigned long long* count, unsigned long long* offset,
                                            char* fname, char* gname, char* dset_name, double* data)
 {
-    if (!h5_read_as(fname, gname, dset_name, rank, count, offset, 8, data)) fprintf(stderr, "HDF5 read: %s\n", g.err);
+    if (guarded("read_data_serial_double_h5",
+                [&]() { return h5_read_as(fname, gname, dset_name, rank, count, offset, 8, data) ? 0 : -1; }) != 0)
+        fprintf(stderr, "HDF5 read: %s\n", g.err);
 }
 
 extern "C" void read_data_serial_float_h5(int rank, unsigned long long* count, unsigned long long* offset,
                                           char* fname, char* gname, char* dset_name, float* data)
 {
-    if (!h5_read_as(fname, gname, dset_name, rank, count, offset, 4, data)) fprintf(stderr, "HDF5 read: %s\n", g.err);
+    if (guarded("read_data_serial_float_h5",
+                [&]() { return h5_read_as(fname, gname, dset_name, rank, count, offset, 4, data) ? 0 : -1; }) != 0)
+        fprintf(stderr, "HDF5 read: %s\n", g.err);
 }
 
 // src/data_io.c:90-120: the file's values from element `offset` on.
@@ -164,7 +188,7 @@ extern "C" void read_data_serial_double_binary(char* fname, long offset, long si
     read_binary(fname, offset, size, data);
 }
 
-extern "C" int tp_h5_write_particles_fields(const char* fname, int write_meta, unsigned long long ntot,
+static int tp_h5_write_particles_fields_impl(const char* fname, int write_meta, unsigned long long ntot,
                                             unsigned long long offset, int nptl, const particles* ptl,
                                             const emfields* emf)
 {
@@ -209,7 +233,7 @@ extern "C" int tp_h5_write_particles_fields(const char* fname, int write_meta, u
 // save_particles_fields, src/diagnostics.c:290-387: this rank's nptl records
 // at offset naccumulate[mpi_rank - 1] (0 for rank 0) of ntot, with the fields
 // at each record's (x, y, z, t) from the library's FP64 get_emf.
-extern "C" int tp_save_particles_fields(int mpi_rank, int nptl, particles* ptl, int ntot, int* naccumulate,
+static int tp_save_particles_fields_impl(int mpi_rank, int nptl, particles* ptl, int ntot, int* naccumulate,
                                         char* fname, int system_type_arg)
 {
     (void)system_type_arg;  // the reference passes it through unused
@@ -236,7 +260,7 @@ extern "C" int tp_save_particles_fields(int mpi_rank, int nptl, particles* ptl, 
 // read_particles, src/particle_info.c:376-443: records [offset, offset + nptl)
 // of /particles_fields/particles into x, y, z, qm, ux, uy, uz, t of ptl (the
 // other members are left as they are), converted from the file's type.
-extern "C" int tp_read_particles(int mpi_rank, int nptl, int* nptl_accumulate, particles* ptl, char* fname)
+static int tp_read_particles_impl(int mpi_rank, int nptl, int* nptl_accumulate, particles* ptl, char* fname)
 {
     if (mpi_rank < 0 || nptl < 0 || (mpi_rank > 0 && !nptl_accumulate) || !fname || (nptl > 0 && !ptl)) {
         set_error(7, "tp_read_particles: bad arguments");
@@ -285,7 +309,7 @@ extern "C" int tp_read_particles(int mpi_rank, int nptl, int* nptl_accumulate, p
 
 // data/poincare_map.h5: /poincare_map/{xpos,ypos,zpos} [npoints_total][ncross + 1]
 // native doubles; this rank's rows [nshift, nshift + npoints).
-extern "C" int tp_h5_write_poincare(const char* fname, int npoints_total, int ncross, int nshift, int npoints,
+static int tp_h5_write_poincare_impl(const char* fname, int npoints_total, int ncross, int nshift, int npoints,
                                     const double* xpos, const double* ypos, const double* zpos)
 {
     if (!fname || npoints_total < 0 || ncross < 0 || nshift < 0 || npoints < 0 || nshift + npoints > npoints_total ||
@@ -319,4 +343,55 @@ extern "C" int tp_h5_write_poincare(const char* fname, int npoints_total, int nc
         return -1;
     }
     return 0;
+}
+
+extern "C" int tp_h5_read(const char* fname, const char* gname, const char* dset, int rank,
+                          const unsigned long long* count, const unsigned long long* offset, int elem_bytes,
+                          void* data)
+{
+    return guarded("tp_h5_read",
+                   [&]() { return tp_h5_read_impl(fname, gname, dset, rank, count, offset, elem_bytes, data); });
+}
+
+extern "C" int tp_h5_info(const char* fname, const char* gname, const char* dset, int* rank,
+                          unsigned long long* dims, int* type_class, int* type_size)
+{
+    return guarded("tp_h5_info",
+                   [&]() { return tp_h5_info_impl(fname, gname, dset, rank, dims, type_class, type_size); });
+}
+
+extern "C" int tp_h5_write_particles_fields(const char* fname, int write_meta, unsigned long long ntot,
+                                            unsigned long long offset, int nptl, const particles* ptl,
+                                            const emfields* emf)
+{
+    return guarded("tp_h5_write_particles_fields",
+                   [&]() {
+                       return tp_h5_write_particles_fields_impl(fname, write_meta, ntot, offset, nptl, ptl, emf);
+                   });
+}
+
+extern "C" int tp_save_particles_fields(int mpi_rank, int nptl, particles* ptl, int ntot, int* naccumulate,
+                                        char* fname, int system_type_arg)
+{
+    return guarded("tp_save_particles_fields",
+                   [&]() {
+                       return tp_save_particles_fields_impl(mpi_rank, nptl, ptl, ntot, naccumulate, fname,
+                                                            system_type_arg);
+                   });
+}
+
+extern "C" int tp_read_particles(int mpi_rank, int nptl, int* nptl_accumulate, particles* ptl, char* fname)
+{
+    return guarded("tp_read_particles",
+                   [&]() { return tp_read_particles_impl(mpi_rank, nptl, nptl_accumulate, ptl, fname); });
+}
+
+extern "C" int tp_h5_write_poincare(const char* fname, int npoints_total, int ncross, int nshift, int npoints,
+                                    const double* xpos, const double* ypos, const double* zpos)
+{
+    return guarded("tp_h5_write_poincare",
+                   [&]() {
+                       return tp_h5_write_poincare_impl(fname, npoints_total, ncross, nshift, npoints, xpos, ypos,
+                                                        zpos);
+                   });
 }

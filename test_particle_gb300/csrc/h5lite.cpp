@@ -230,7 +230,8 @@ Type Type::compound_f64(const std::vector<std::string>& names, bool big_endian)
     Type t;
     t.cls = 6;
     t.size = (uint32_t)(8 * names.size());
-    for (size_t i = 0; i < names.size(); i++) t.members.push_back(Member{names[i], (uint32_t)(8 * i), {1, 8, big_endian, true}});
+    for (size_t i = 0; i < names.size(); i++)
+        t.members.push_back(Member{names[i], (uint32_t)(8 * i), {1, 8, big_endian, true}});
     return t;
 }
 
@@ -396,7 +397,7 @@ bool File::messages(uint64_t oh, std::vector<Msg>& out)
 bool File::btree_entries(uint64_t node, uint64_t heap_data, uint64_t heap_size, const std::string& name,
                          uint64_t& oh, int depth)
 {
-    if (depth > 32) return fail("group B-tree too deep");
+    if (depth > 32 || ++visits_ > (1u << 20)) return fail("group B-tree too deep or cyclic");
     uint8_t h[24];
     if (!rd(node, h, 24)) return false;
     if (memcmp(h, "TREE", 4) || h[4] != 0) return fail("bad group B-tree node at %llu", (unsigned long long)node);
@@ -436,7 +437,8 @@ bool File::group_entry(uint64_t group_oh, const std::string& name, uint64_t& oh)
     std::vector<Msg> ms;
     if (!messages(group_oh, ms)) return false;
     for (const Msg& m : ms) {
-        if (m.type == 0x06 || m.type == 0x02) return fail("group with link messages (the newer file format): not supported");
+        if (m.type == 0x06 || m.type == 0x02)
+            return fail("group with link messages (the newer file format): not supported");
         if (m.type != 0x11) continue;
         if (m.data.size() < 16) return fail("bad symbol table message");
         const uint64_t bt = le(&m.data[0], 8), hp = le(&m.data[8], 8);
@@ -444,6 +446,7 @@ bool File::group_entry(uint64_t group_oh, const std::string& name, uint64_t& oh)
         if (!rd(hp, hh, 32)) return false;
         if (memcmp(hh, "HEAP", 4)) return fail("bad local heap at %llu", (unsigned long long)hp);
         oh = kUndef;
+        visits_ = 0;
         if (!btree_entries(bt, le(hh + 24, 8), le(hh + 8, 8), name, oh, 0)) return false;
         if (oh == kUndef) return fail("no object named '%s'", name.c_str());
         return true;
@@ -557,6 +560,14 @@ bool File::dataset(const char* group, const char* name, Dataset& ds)
         }
     }
     if (!have_space || !have_type || ds.layout < 0) return fail("'%s' is not a dataset", path.c_str());
+    if (ds.type.size == 0 || ds.dims.size() > 32) return fail("bad datatype size or rank");
+    {
+        uint64_t n = 1;
+        for (uint64_t d : ds.dims) {
+            if (d != 0 && n > (~0ull >> 2) / d / ds.type.size) return fail("dataset extent overflows");
+            n *= d;
+        }
+    }
     if (ds.layout == 2 && ds.chunk.size() != ds.dims.size()) return fail("chunk rank differs from the dataspace's");
     if (ds.layout == 1 && ds.bytes == 0 && ds.addr != kUndef) ds.bytes = ds.elements() * ds.type.size;
     if (fill.size() == ds.type.size) ds.fill = fill;
@@ -566,7 +577,7 @@ bool File::dataset(const char* group, const char* name, Dataset& ds)
 bool File::chunk_index(const Dataset& ds, uint64_t node, int depth, std::vector<uint64_t>& keys,
                        std::vector<uint64_t>& addrs, std::vector<uint32_t>& sizes)
 {
-    if (depth > 32) return fail("chunk B-tree too deep");
+    if (depth > 32 || ++visits_ > (1u << 20)) return fail("chunk B-tree too deep or cyclic");
     uint8_t h[24];
     if (!rd(node, h, 24)) return false;
     if (memcmp(h, "TREE", 4) || h[4] != 1) return fail("bad chunk B-tree node at %llu", (unsigned long long)node);
@@ -646,13 +657,16 @@ bool File::read(const Dataset& ds, const uint64_t* offset, const uint64_t* count
     // chunked: every stored chunk that meets the selection
     std::vector<uint64_t> keys, addrs;
     std::vector<uint32_t> sizes;
+    visits_ = 0;
     if (ds.addr != kUndef && !chunk_index(ds, ds.addr, 0, keys, addrs, sizes)) return false;
     std::map<std::vector<uint64_t>, size_t> where;
-    for (size_t c = 0; c < addrs.size(); c++) where[std::vector<uint64_t>(keys.begin() + c * r, keys.begin() + (c + 1) * r)] = c;
+    for (size_t c = 0; c < addrs.size(); c++)
+        where[std::vector<uint64_t>(keys.begin() + c * r, keys.begin() + (c + 1) * r)] = c;
     uint64_t celems = 1;
     for (size_t d = 0; d < r; d++) {
         if (ds.chunk[d] == 0) return fail("zero chunk extent");
         celems *= ds.chunk[d];
+        if (celems * es > size_) return fail("chunk larger than the file");  // also bounds the product
     }
     std::vector<uint8_t> cbuf(celems * es);
     std::vector<uint64_t> first(r), last(r), ci(r);

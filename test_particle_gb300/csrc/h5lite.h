@@ -104,6 +104,7 @@ private:
     uint64_t base_ = 0;
     uint64_t size_ = 0;
     uint64_t root_ = kUndef;
+    uint64_t visits_ = 0;  // B-tree nodes visited by the current lookup (bounded)
     std::string path_;
     std::string err_;
     bool fail(const char* fmt, ...);

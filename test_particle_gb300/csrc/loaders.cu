@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 
 #include "../../include/tp_gpu.h"
 #include "../../include/tp_h5.h"
@@ -206,7 +207,7 @@ extern "C" int tp_fetch_device_fields(float* host_e, float* host_b)
 // file in whole i-planes through two pinned buffers (reading the next piece
 // while the previous one copies), then one transpose kernel writes the
 // component into the records.
-extern "C" int tp_read_pic_fields_h5(const char* fname, const char* gname, int with_e)
+static int read_pic_fields_h5_impl(const char* fname, const char* gname, int with_e)
 {
     if (!ensure_init()) return -1;
     if (multi_tframe != 0) {
@@ -294,4 +295,16 @@ extern "C" int tp_read_pic_fields_h5(const char* fname, const char* gname, int w
     }
     g.upload_gen++;
     return cuda_ok(cudaStreamSynchronize(s), "field read") ? 0 : fail();
+}
+
+extern "C" int tp_read_pic_fields_h5(const char* fname, const char* gname, int with_e)
+{
+    try {
+        return read_pic_fields_h5_impl(fname, gname, with_e);
+    } catch (const std::exception& e) {  // e.g. an allocation for a corrupted extent
+        set_error(7, "tp_read_pic_fields_h5: %s", e.what());
+    } catch (...) {
+        set_error(7, "tp_read_pic_fields_h5 failed");
+    }
+    return -1;
 }

@@ -369,3 +369,57 @@ def test_filtered_chunks_are_refused(lib, tmp_path):
     open(fn, "wb").write(bytes(b))
     rc, _ = _read(lib, fn, "/", "d", [0, 0], [4, 6])
     assert rc == -1 and "filtered chunk" in _err(lib)
+
+
+_FUZZ_CHILD = r"""
+import ctypes as C, os, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import test_particle_gb300 as tp
+L = tp.lib()
+src, work, seed, n = sys.argv[2], sys.argv[3], int(sys.argv[4]), int(sys.argv[5])
+base = bytearray(open(src, "rb").read())
+rng = np.random.default_rng(seed)
+ok = err = 0
+for it in range(n):
+    b = bytearray(base)
+    for _ in range(int(rng.integers(1, 4))):
+        i = int(rng.integers(0, len(b)))
+        b[i] = int(rng.integers(0, 256)) if rng.random() < 0.7 else b[i] ^ (1 << int(rng.integers(0, 8)))
+    open(work, "wb").write(bytes(b))
+    for grp, name in (("/Timestep_3/sub", "cbx"), ("/", "top")):
+        rank, cls, size = C.c_int(), C.c_int(), C.c_int()
+        dims = (C.c_ulonglong * 32)()
+        if L.tp_h5_info(work.encode(), grp.encode(), name.encode(), C.byref(rank), dims, C.byref(cls),
+                        C.byref(size)) != 0:
+            err += 1
+            continue
+        r = rank.value
+        cnt = [min(int(dims[d]), 16) for d in range(r)]
+        out = np.zeros(max(int(np.prod(cnt)) if r else 1, 1))
+        rc = L.tp_h5_read(work.encode(), grp.encode(), name.encode(), r, (C.c_ulonglong * max(r, 1))(*cnt),
+                          (C.c_ulonglong * max(r, 1))(*([0] * r)), 8, out.ctypes.data_as(C.c_void_p))
+        ok += rc == 0
+        err += rc != 0
+    q = np.zeros(4, dtype=tp.PARTICLE_DTYPE)
+    L.tp_read_particles(0, 4, None, q.ctypes.data_as(C.c_void_p), work.encode())
+print("FUZZ", ok, err)
+"""
+
+
+@pytest.mark.parametrize("layout", ["contiguous", "chunked"])
+def test_corrupted_files_give_errors_not_crashes(lib, tmp_path, layout):
+    """Random byte changes anywhere in a file: every call returns data or an
+    error status (run in a child process, so a crash fails the test)."""
+    import subprocess
+    rng = np.random.default_rng(14)
+    fn = str(tmp_path / "base.h5")
+    kw = {"layout": "chunked", "chunks": {"Timestep_3/sub/cbx": (3, 4, 5), "top": (4,)}} if layout == "chunked" else {}
+    h5ref.write(fn, {"top": rng.normal(size=11), "Timestep_3": {"sub": {"cbx": rng.normal(size=(7, 9, 10))}}}, **kw)
+    r = subprocess.run([sys.executable, "-c", _FUZZ_CHILD, ROOT, fn, str(tmp_path / "work.h5"), "15", "600"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("FUZZ")]
+    assert line, r.stdout[-2000:]
+    ok, err = (int(v) for v in line[0].split()[1:])
+    assert ok > 0 and err > 0
