@@ -2,9 +2,10 @@
  * tp_h5.h -- the reference's HDF5 files, read and written by libtpgpu.so
  * without libhdf5 (the file format's earliest version, the one libhdf5 writes
  * by default and the reference's files use: version 0/1 superblock, version 1
- * object headers, symbol-table groups, contiguous, compact or unfiltered
- * chunked datasets).  Files in the newer format, or with compressed data, are
- * refused with the reason in tp_last_error().
+ * object headers, symbol-table groups, contiguous, compact or chunked
+ * datasets, chunks through deflate (the system's zlib, loaded at run time),
+ * shuffle and Fletcher-32).  Files in the newer format, or with other filters,
+ * are refused with the reason in tp_last_error().
  *
  * Reference locations are paths inside the reference project.
  */

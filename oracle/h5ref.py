@@ -194,12 +194,52 @@ class File:
                     sz = _u(body, 2, 4)
                     fill = body[6:6 + sz]
             elif t == 0x0B:
-                filtered = body[1] > 0
+                filtered = self._filters(body)
             elif t == 0x08:
                 layout = self._layout(body)
         if dims is None or layout is None:
             raise H5Error("%s is not a dataset" % path)
         return dims, dt, layout, fill, filtered
+
+    @staticmethod
+    def _filters(body):
+        ver, n = body[0], body[1]
+        p = 8 if ver == 1 else 2
+        out = []
+        for _ in range(n):
+            fid = _u(body, p, 2)
+            p += 2
+            namelen = 0
+            if ver == 1 or fid >= 256:
+                namelen = _u(body, p, 2)
+                p += 2
+            p += 2  # flags
+            ncd = _u(body, p, 2)
+            p += 2
+            p += ((namelen + 7) // 8) * 8 if ver == 1 else namelen
+            cd = [_u(body, p + 4 * i, 4) for i in range(ncd)]
+            p += 4 * ncd + (4 if ver == 1 and ncd % 2 else 0)
+            out.append((fid, cd))
+        return out
+
+    @staticmethod
+    def _unfilter(raw, filters, mask, itemsize):
+        import zlib
+        for i in range(len(filters) - 1, -1, -1):
+            if mask >> i & 1:
+                continue
+            fid, cd = filters[i]
+            if fid == 1:
+                raw = zlib.decompress(raw)
+            elif fid == 2:
+                es = cd[0] if cd else itemsize
+                ne = len(raw) // es
+                raw = np.frombuffer(raw[:ne * es], np.uint8).reshape(es, ne).T.tobytes() + raw[ne * es:]
+            elif fid == 3:
+                raw = raw[:-4]
+            else:
+                raise H5Error("filter %d" % fid)
+        return raw
 
     @staticmethod
     def _layout(body):
@@ -243,14 +283,15 @@ class File:
                 return self._filled(shape, dt, fill)
             a = self._a(layout[1])
             return np.frombuffer(self.b, dtype=dt, count=n, offset=a).reshape(shape).copy()
-        if filtered:
-            raise H5Error("filtered chunks")
         out = self._filled(shape, dt, fill)
         cdims = layout[2]
+        n_c = int(np.prod(cdims))
         if layout[1] != UNDEF:
-            for offs, addr in self._btree_chunks(layout[1], len(dims)):
-                chunk = np.frombuffer(self.b, dtype=dt, count=int(np.prod(cdims)),
-                                      offset=self._a(addr)).reshape(cdims)
+            for offs, addr, size, mask in self._btree_chunks(layout[1], len(dims), bool(filtered)):
+                raw = self.b[self._a(addr):self._a(addr) + (size if filtered else n_c * dt.itemsize)]
+                if filtered:
+                    raw = self._unfilter(raw, filtered, mask, dt.itemsize)
+                chunk = np.frombuffer(raw, dtype=dt, count=n_c).reshape(cdims)
                 dst = tuple(slice(o, min(o + c, d)) for o, c, d in zip(offs, cdims, dims))
                 src = tuple(slice(0, s.stop - s.start) for s in dst)
                 out[dst] = chunk[src]
@@ -263,7 +304,7 @@ class File:
             out[...] = np.frombuffer(fill, dtype=dt)[0]
         return out
 
-    def _btree_chunks(self, node, rank):
+    def _btree_chunks(self, node, rank, filtered=False):
         a = self._a(node)
         if self.b[a:a + 4] != b"TREE" or self.b[a + 4] != 1:
             raise H5Error("chunk B-tree")
@@ -273,11 +314,12 @@ class File:
             k = a + 24 + i * (ks + 8)
             child = _u(self.b, k + ks, 8)
             if level > 0:
-                yield from self._btree_chunks(child, rank)
+                yield from self._btree_chunks(child, rank, filtered)
             else:
-                if _u(self.b, k + 4, 4):
+                mask = _u(self.b, k + 4, 4)
+                if mask and not filtered:
                     raise H5Error("filtered chunk")
-                yield [_u(self.b, k + 8 + 8 * d, 8) for d in range(rank)], child
+                yield [_u(self.b, k + 8 + 8 * d, 8) for d in range(rank)], child, _u(self.b, k, 4), mask
 
 
 def read(path, dset):
@@ -344,7 +386,7 @@ def _msg(t, body, flags=0):
 
 def write(path, tree, *, userblock=0, superblock=0, layout="contiguous", layout_version=3, chunks=None,
           drop_chunks=(), fill=None, split_header=False, dataspace_version=1, compound_version=1,
-          chunk_leaf_entries=64):
+          chunk_leaf_entries=64, filters=(), unfiltered_chunks=()):
     """Write `tree` ({name: ndarray or nested dict}) as an HDF5 file; addresses
     are relative to the user block's end (the base address)."""
     o = _Out(b"")
@@ -391,7 +433,9 @@ def write(path, tree, *, userblock=0, superblock=0, layout="contiguous", layout_
                 lm += b"".join(struct.pack("<I", d) for d in arr.shape) + struct.pack("<I", dt.itemsize)
         else:
             cd = list(chunks[name_path] if isinstance(chunks, dict) else chunks)
-            bt = _write_chunks(o, ub, arr, cd, drop_chunks, chunk_leaf_entries)
+            bt = _write_chunks(o, ub, arr, cd, drop_chunks, chunk_leaf_entries, filters, unfiltered_chunks)
+            if filters:
+                msgs.append(_msg(0x0B, _pipeline(filters, dt.itemsize), 1))
             if layout_version == 3:
                 lm = bytes([3, 2, rank + 1]) + struct.pack("<Q", bt)
             else:
@@ -476,10 +520,42 @@ def _object_header(o, ub, msgs, split):
     return a - ub
 
 
-def _write_chunks(o, ub, arr, cd, drop, leaf_entries):
-    """Chunks of arr (edge chunks stored whole, padded with zeros) and a
-    version 1 B-tree over them: leaves of up to leaf_entries chunks under one
-    level-1 node when there are more."""
+_FILTER_IDS = {"deflate": 1, "shuffle": 2, "fletcher32": 3}
+
+
+def _pipeline(filters, itemsize):
+    """Filter pipeline message version 1 (names padded to 8, client data
+    padded to an even count)."""
+    out = bytes([1, len(filters)]) + b"\0" * 6
+    for name in filters:
+        cd = {"deflate": [6], "shuffle": [itemsize], "fletcher32": []}[name]
+        nm = name.encode() + b"\0"
+        nm += b"\0" * (-len(nm) % 8)
+        out += struct.pack("<HHHH", _FILTER_IDS[name], len(nm), 1 if name == "deflate" else 0, len(cd)) + nm
+        out += b"".join(struct.pack("<I", v) for v in cd) + (b"\0" * 4 if len(cd) % 2 else b"")
+    return out
+
+
+def _apply_filters(raw, filters, itemsize, mask):
+    import zlib
+    for i, name in enumerate(filters):
+        if mask >> i & 1:
+            continue
+        if name == "shuffle":
+            ne = len(raw) // itemsize
+            raw = np.frombuffer(raw[:ne * itemsize], np.uint8).reshape(ne, itemsize).T.tobytes() + raw[ne * itemsize:]
+        elif name == "deflate":
+            raw = zlib.compress(raw, 6)
+        elif name == "fletcher32":
+            raw = raw + b"\0\0\0\0"  # the reader strips the checksum without checking it
+    return raw
+
+
+def _write_chunks(o, ub, arr, cd, drop, leaf_entries, filters=(), unfiltered=()):
+    """Chunks of arr (edge chunks stored whole, padded with zeros), through
+    the filters in order (a chunk listed in `unfiltered` skips them all, as
+    its filter mask says), and a version 1 B-tree over them: leaves of up to
+    leaf_entries chunks under one level-1 node when there are more."""
     rank = arr.ndim
     grid = [-(-s // c) for s, c in zip(arr.shape, cd)]
     recs = []
@@ -490,14 +566,15 @@ def _write_chunks(o, ub, arr, cd, drop, leaf_entries):
         block = np.zeros(cd, dtype=arr.dtype)
         sl = tuple(slice(lo_, min(lo_ + c, s)) for lo_, c, s in zip(lo, cd, arr.shape))
         block[tuple(slice(0, x.stop - x.start) for x in sl)] = arr[sl]
-        raw = block.tobytes()
+        mask = (1 << len(filters)) - 1 if idx in unfiltered else 0
+        raw = _apply_filters(block.tobytes(), filters, arr.dtype.itemsize, mask)
         a = o.alloc(len(raw), 16)
         o.put(a, raw)
-        recs.append((lo, a - ub, len(raw)))
+        recs.append((lo, a - ub, len(raw), mask))
     ks = 8 + 8 * (rank + 1)
 
-    def key(lo, size):
-        return struct.pack("<II", size, 0) + b"".join(struct.pack("<Q", x) for x in lo) + struct.pack("<Q", 0)
+    def key(lo, size, mask=0):
+        return struct.pack("<II", size, mask) + b"".join(struct.pack("<Q", x) for x in lo) + struct.pack("<Q", 0)
 
     def node(level, items, right_key):
         body = b"TREE" + bytes([1, level]) + struct.pack("<HQQ", len(items), UNDEF, UNDEF)
@@ -512,7 +589,8 @@ def _write_chunks(o, ub, arr, cd, drop, leaf_entries):
     leaves = []
     for s0 in range(0, len(recs), leaf_entries):
         part = recs[s0:s0 + leaf_entries]
-        leaves.append((key(part[0][0], part[0][2]), node(0, [(key(lo, sz), a) for lo, a, sz in part], end_key)))
+        leaves.append((key(part[0][0], part[0][2], part[0][3]),
+                       node(0, [(key(lo, sz, m), a) for lo, a, sz, m in part], end_key)))
     if not leaves:
         return node(0, [], end_key)
     if len(leaves) == 1:

@@ -70,7 +70,7 @@ def build(force=False, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, UNITS))
     tmp = LIB + ".%d.tmp" % os.getpid()
-    cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static"]
+    cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

@@ -6,6 +6,7 @@
 // metadata integers are little-endian; offsets and lengths are 8 bytes.
 #include "h5lite.h"
 
+#include <dlfcn.h>
 #include <fcntl.h>
 #include <unistd.h>
 
@@ -514,9 +515,22 @@ bool File::dataset(const char* group, const char* name, Dataset& ds)
             }
             break;
         }
-        case 0x0b: {  // filter pipeline
+        case 0x0b: {  // filter pipeline: id, [name length], flags, client data count, [name], client data
             const int ver = (int)c.u(1), n = (int)c.u(1);
-            if ((ver == 1 || ver == 2) && n > 0) ds.filtered = true;
+            if (ver != 1 && ver != 2) return fail("filter pipeline message version %d", ver);
+            if (ver == 1) c.skip(6);
+            for (int i = 0; i < n && c.ok; i++) {
+                tph5::Filter fl;
+                fl.id = (uint16_t)c.u(2);
+                const uint32_t namelen = (ver == 1 || fl.id >= 256) ? (uint32_t)c.u(2) : 0u;
+                fl.flags = (uint16_t)c.u(2);
+                const uint32_t ncd = (uint32_t)c.u(2);
+                c.skip(ver == 1 ? pad8(namelen) : namelen);
+                for (uint32_t v = 0; v < ncd; v++) fl.cd.push_back((uint32_t)c.u(4));
+                if (ver == 1 && (ncd & 1)) c.skip(4);
+                ds.filters.push_back(fl);
+            }
+            if (!c.ok) return fail("bad filter pipeline message");
             break;
         }
         case 0x08: {  // data layout
@@ -574,8 +588,60 @@ bool File::dataset(const char* group, const char* name, Dataset& ds)
     return true;
 }
 
+namespace {
+
+// zlib's uncompress(dest, &destLen, source, sourceLen), from the system's
+// libz, looked up once at first use.
+using uncompress_fn = int (*)(unsigned char*, unsigned long*, const unsigned char*, unsigned long);
+uncompress_fn zlib_uncompress()
+{
+    static uncompress_fn fn = []() -> uncompress_fn {
+        void* h = dlopen("libz.so.1", RTLD_NOW | RTLD_LOCAL);
+        if (!h) h = dlopen("libz.so", RTLD_NOW | RTLD_LOCAL);
+        return h ? (uncompress_fn)dlsym(h, "uncompress") : nullptr;
+    }();
+    return fn;
+}
+
+}  // namespace
+
+// Undoes the filters of one stored chunk, last first (a set bit i of `mask`:
+// filter i was skipped for this chunk); `want` is the chunk's size.
+bool File::unfilter(const Dataset& ds, uint32_t mask, std::vector<uint8_t>& buf, size_t want)
+{
+    for (size_t i = ds.filters.size(); i-- > 0;) {
+        if (mask & (1u << i)) continue;
+        const Filter& fl = ds.filters[i];
+        if (fl.id == 1) {  // deflate
+            uncompress_fn unz = zlib_uncompress();
+            if (!unz) return fail("deflate-compressed chunks need the system's zlib (libz.so.1), not found");
+            std::vector<uint8_t> out(want);
+            unsigned long n = (unsigned long)want;
+            if (unz(out.data(), &n, buf.data(), (unsigned long)buf.size()) != 0 || n != want)
+                return fail("a deflate-compressed chunk does not inflate to %zu bytes", want);
+            buf.swap(out);
+        } else if (fl.id == 2) {  // shuffle: byte b of every element stored together
+            const size_t es = fl.cd.empty() ? ds.type.size : fl.cd[0];
+            if (es > 1) {
+                const size_t ne = buf.size() / es;
+                std::vector<uint8_t> out(buf);
+                for (size_t e = 0; e < ne; e++)
+                    for (size_t b = 0; b < es; b++) out[e * es + b] = buf[b * ne + e];
+                buf.swap(out);
+            }
+        } else if (fl.id == 3) {  // Fletcher-32: a 4-byte checksum after the data
+            if (buf.size() < 4) return fail("chunk shorter than its checksum");
+            buf.resize(buf.size() - 4);
+        } else {
+            return fail("filter %u: not supported", (unsigned)fl.id);
+        }
+    }
+    if (buf.size() < want) return fail("short chunk");
+    return true;
+}
+
 bool File::chunk_index(const Dataset& ds, uint64_t node, int depth, std::vector<uint64_t>& keys,
-                       std::vector<uint64_t>& addrs, std::vector<uint32_t>& sizes)
+                       std::vector<uint64_t>& addrs, std::vector<uint32_t>& sizes, std::vector<uint32_t>& masks)
 {
     if (depth > 32 || ++visits_ > (1u << 20)) return fail("chunk B-tree too deep or cyclic");
     uint8_t h[24];
@@ -589,13 +655,15 @@ bool File::chunk_index(const Dataset& ds, uint64_t node, int depth, std::vector<
         const uint8_t* k = &kc[(size_t)i * (ksz + 8)];
         const uint64_t child = le(k + ksz, 8);
         if (level > 0) {
-            if (!chunk_index(ds, child, depth + 1, keys, addrs, sizes)) return false;
+            if (!chunk_index(ds, child, depth + 1, keys, addrs, sizes, masks)) return false;
             continue;
         }
-        if (le(k + 4, 4) != 0) return fail("filtered chunk: not supported");
+        const uint32_t mask = (uint32_t)le(k + 4, 4);
+        if (ds.filters.empty() && mask != 0) return fail("filtered chunk without a filter pipeline");
         for (size_t d = 0; d < ds.dims.size(); d++) keys.push_back(le(k + 8 + 8 * d, 8));
         addrs.push_back(child);
         sizes.push_back((uint32_t)le(k, 4));
+        masks.push_back(mask);
     }
     return true;
 }
@@ -611,7 +679,7 @@ bool File::read(const Dataset& ds, const uint64_t* offset, const uint64_t* count
     }
     uint8_t* out = (uint8_t*)raw;
     if (total == 0) return true;
-    if (ds.filtered) return fail("compressed or filtered dataset: not supported");
+    if (!ds.filters.empty() && ds.layout != 2) return fail("filters on a dataset that is not chunked");
     // elements in dimensions d.. of the dataset and of the selection (the
     // stride of dimension d is entry d + 1)
     std::vector<uint64_t> dstride(r + 1, 1), sstride(r + 1, 1);
@@ -656,9 +724,9 @@ bool File::read(const Dataset& ds, const uint64_t* offset, const uint64_t* count
     }
     // chunked: every stored chunk that meets the selection
     std::vector<uint64_t> keys, addrs;
-    std::vector<uint32_t> sizes;
+    std::vector<uint32_t> sizes, masks;
     visits_ = 0;
-    if (ds.addr != kUndef && !chunk_index(ds, ds.addr, 0, keys, addrs, sizes)) return false;
+    if (ds.addr != kUndef && !chunk_index(ds, ds.addr, 0, keys, addrs, sizes, masks)) return false;
     std::map<std::vector<uint64_t>, size_t> where;
     for (size_t c = 0; c < addrs.size(); c++)
         where[std::vector<uint64_t>(keys.begin() + c * r, keys.begin() + (c + 1) * r)] = c;
@@ -683,9 +751,16 @@ bool File::read(const Dataset& ds, const uint64_t* offset, const uint64_t* count
             for (uint64_t i = 0; i < celems; i++)
                 if (!ds.fill.empty()) memcpy(&cbuf[i * es], ds.fill.data(), es);
                 else memset(&cbuf[i * es], 0, es);
-        } else {
+        } else if (ds.filters.empty()) {
             if (sizes[it->second] < cbuf.size()) return fail("short chunk");
             if (!rd(addrs[it->second], cbuf.data(), cbuf.size())) return false;
+        } else {
+            const size_t want = cbuf.size();
+            if (sizes[it->second] > size_) return fail("stored chunk larger than the file");
+            cbuf.resize(sizes[it->second]);
+            if (!rd(addrs[it->second], cbuf.data(), cbuf.size()) || !unfilter(ds, masks[it->second], cbuf, want))
+                return false;
+            cbuf.resize(want);
         }
         // copy the part of this chunk inside the selection, element rows of the last dimension
         std::vector<uint64_t> lo(r), hi(r);

@@ -19,10 +19,11 @@
 // with continuation blocks, symbol-table groups, dataspace messages 1 and 2,
 // fixed-point, floating-point and compound datatypes (versions 1 to 3),
 // layout messages 1 to 3 (compact, contiguous, chunked with a version 1
-// B-tree and no filters) and contiguous or compact layout version 4.  Files in
-// the newer format (superblock 2 and 3, version 2 object headers, link
-// messages, compressed chunks) are refused with a message saying so.  The
-// writer emits the earliest format, as libhdf5 does by default.
+// B-tree; chunks through the deflate, shuffle and Fletcher-32 filters) and
+// contiguous or compact layout version 4.  Files in the newer format
+// (superblock 2 and 3, version 2 object headers, link messages) and other
+// filters are refused with a message saying so.  The writer emits the
+// earliest format, as libhdf5 does by default.
 //
 // Layout of a written file: superblock, then every group's object header,
 // B-tree node, local heap and symbol-table node, then the datasets' object
@@ -66,6 +67,13 @@ struct Type {
     static Type compound_f64(const std::vector<std::string>& names, bool big_endian);
 };
 
+// One stage of a chunked dataset's filter pipeline.
+struct Filter {
+    uint16_t id = 0;  // 1 deflate, 2 shuffle, 3 Fletcher-32 (others are refused on read)
+    uint16_t flags = 0;
+    std::vector<uint32_t> cd;  // client data
+};
+
 struct Dataset {
     std::vector<uint64_t> dims;
     Type type;
@@ -75,7 +83,7 @@ struct Dataset {
     std::vector<uint8_t> compact;  // compact layout: the data
     std::vector<uint8_t> fill;     // the fill value, when the file defines one
     std::vector<uint64_t> chunk;   // chunk extent per dimension
-    bool filtered = false;
+    std::vector<Filter> filters;   // chunked data: applied in order on write, undone in reverse on read
     uint64_t elements() const;
 };
 
@@ -91,6 +99,9 @@ public:
     bool dataset(const char* group, const char* name, Dataset& ds);
     // The hyperslab [offset, offset + count) of every dimension, as the file's
     // raw element bytes in C order (elements() * type.size bytes for the whole).
+    // Chunks stored through deflate (with the system's zlib, loaded at run
+    // time), shuffle and Fletcher-32 filters are undone; other filters are
+    // refused.
     bool read(const Dataset& ds, const uint64_t* offset, const uint64_t* count, void* raw);
     const std::string& error() const { return err_; }
 
@@ -114,7 +125,8 @@ private:
     bool btree_entries(uint64_t node, uint64_t heap_data, uint64_t heap_size, const std::string& name,
                        uint64_t& oh, int depth);
     bool chunk_index(const Dataset& ds, uint64_t node, int depth, std::vector<uint64_t>& keys,
-                     std::vector<uint64_t>& addrs, std::vector<uint32_t>& sizes);
+                     std::vector<uint64_t>& addrs, std::vector<uint32_t>& sizes, std::vector<uint32_t>& masks);
+    bool unfilter(const Dataset& ds, uint32_t mask, std::vector<uint8_t>& buf, size_t want);
 };
 
 // Element conversion, as a C cast from the decoded value: floats exactly,

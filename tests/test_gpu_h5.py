@@ -34,6 +34,7 @@ def _c_order(comp, nx, ny, nz):
     (">f8", {"split_header": True}),
     ("<f4", {"pad": (3, 1, 2)}),
     ("<f4", {"layout": "compact"}),
+    ("<f4", {"layout": "chunked", "chunks": (4, 4, 4), "filters": ("shuffle", "deflate")}),
 ])
 def test_records_match_reference_reader(tmp_path, dtype, kw):
     f, ct, _, _ = gf.setup(tmp_path)

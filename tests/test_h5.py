@@ -254,6 +254,10 @@ VARIANTS = {
                                       fill=7.0),
     "chunked_two_level_btree": dict(layout="chunked", chunks=(1, 2, 3), chunk_leaf_entries=5),
     "split_header": dict(split_header=True, fill=1.0),
+    "chunked_deflate": dict(layout="chunked", chunks=(3, 5, 4), filters=("deflate",)),
+    "chunked_shuffle_deflate_fletcher32": dict(layout="chunked", chunks=(4, 4, 4),
+                                               filters=("shuffle", "deflate", "fletcher32"),
+                                               unfiltered_chunks={(0, 0, 0), (1, 1, 1)}),
 }
 
 
@@ -423,3 +427,18 @@ def test_corrupted_files_give_errors_not_crashes(lib, tmp_path, layout):
     assert line, r.stdout[-2000:]
     ok, err = (int(v) for v in line[0].split()[1:])
     assert ok > 0 and err > 0
+
+
+def test_unknown_filters_are_refused(lib, tmp_path):
+    """A chunk filter other than deflate, shuffle and Fletcher-32 (here the
+    id of a third-party compressor): refused with its number."""
+    fn = str(tmp_path / "u.h5")
+    h5ref.write(fn, {"d": np.arange(24.0).reshape(4, 6)}, layout="chunked", chunks=(2, 3), filters=("deflate",))
+    b = bytearray(open(fn, "rb").read())
+    at = b.index(b"deflate\0") - 8  # the filter's id field
+    assert int.from_bytes(b[at:at + 2], "little") == 1
+    b[at:at + 2] = (32001).to_bytes(2, "little")
+    open(fn, "wb").write(bytes(b))
+    rc, _ = _read(lib, fn, "/", "d", [0, 0], [4, 6])
+    assert rc == -1 and "filter 32001" in _err(lib)
+    assert _info(lib, fn, "/", "d")[0] == 0  # the dataset's description still reads
