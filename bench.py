@@ -854,6 +854,119 @@ def open_box(tp, wl, args):
             "speedup": rates["one_launch"]["kernel_ms"] / rates["compacted"]["kernel_ms"]}
 
 
+def io_files(tp, wl, args):
+    """The field and particle files of the headline workload through the
+    library: the 512^3 field written as the reference's
+    PIC HDF5 file (6 float datasets, 3.2 GB) and as .gda files, read back into
+    device memory (records identical to the synthesised ones), against the
+    reference's CPU path for the same file (the dataset read, then its serial
+    reorder loop, restated in the oracle, timed per component); and
+    particles_fields_init.h5 of the 1,048,576 particles written with the GPU
+    get_emf and read back, against the reference's serial get_emf loop (the
+    oracle on a sample) plus the write of the same bytes.  Files in a
+    temporary directory, in the page cache when read."""
+    import ctypes as C
+    import shutil
+    cfg = wl.config_grid()
+    dom, grd, p0, _, _ = setup_grid(tp, wl, cfg, 0)
+    L = tp.lib()
+    L.set_variables_bfield(C.byref(grd), C.byref(dom), C.c_double(1.0), C.c_int(0), C.c_int(4))
+    L.set_variables_efield(C.byref(grd), C.byref(dom), C.c_double(1.0), C.c_int(0), C.c_int(4))
+    he, hb = tp.fetch_device_fields()
+    n = cfg["n"]
+    nbytes = 6 * 4 * n ** 3
+    work = tempfile.mkdtemp(prefix="tp_io_")
+    out = {"workload": "pic_%dcube_fields_and_%dptl_particles_fields" % (n, cfg["nptl"]), "dir_in_page_cache": True}
+    try:
+        h5 = os.path.join(work, "fields_0.h5")
+        t0 = time.perf_counter()
+        tp.save_pic_fields_h5(h5, "Timestep_0")
+        t_save = time.perf_counter() - t0
+        for c, name in enumerate(("bx", "by", "bz", "ex", "ey", "ez")):
+            (hb if c < 3 else he)[:, c % 3].tofile(os.path.join(work, "%s_0.gda" % name))
+        tp.release_device_fields()
+        walls = {}
+        for kind in ("binary", "h5", "binary", "h5"):
+            t0 = time.perf_counter()
+            if kind == "h5":
+                tp.read_pic_fields_h5(h5, "Timestep_0")
+            else:
+                tp.read_pic_fields_binary(work + "/", 0)
+            walls[kind] = time.perf_counter() - t0  # the second of each: files cached
+            if kind == "h5":
+                e2, b2 = tp.fetch_device_fields()
+                same = bool(np.array_equal(e2, he) and np.array_equal(b2, hb))
+                del e2, b2
+            tp.release_device_fields()
+        # the reference's CPU path for one component: read the dataset, reorder (serial)
+        from oracle import h5ref
+        from oracle import pyoracle as po
+        po.build_oracle()
+        f = h5ref.File(h5)
+        addr = f.info("/Timestep_0/cbx")[2][1]
+        base = f.base
+        del f
+        rec = np.zeros((n ** 3, 3), np.float32)
+        t0 = time.perf_counter()
+        data = np.fromfile(h5, dtype="<f4", count=n ** 3, offset=base + addr).reshape(n, n, n)
+        t_read = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        po.pic_records_from_c(data, 1.0, 0, rec)
+        t_loop = time.perf_counter() - t0
+        ref_same = bool(np.array_equal(rec[:, 0], hb[:, 0]))
+        del data, rec
+        cpu_s = 6 * (t_read + t_loop)
+        out["f2"] = {"file_gb": nbytes / 1e9,
+                     "save_h5_s": t_save, "save_h5_gbs": nbytes / t_save / 1e9,
+                     "load_h5_s": walls["h5"], "load_h5_gbs": nbytes / walls["h5"] / 1e9,
+                     "load_binary_s": walls["binary"], "load_binary_gbs": nbytes / walls["binary"] / 1e9,
+                     "records_identical": same,
+                     "cpu_reference_path": {"s": cpu_s, "gbs": nbytes / cpu_s / 1e9, "cores": 1,
+                                            "kind": "port", "read_s_per_component": t_read,
+                                            "reorder_s_per_component": t_loop,
+                                            "records_identical": ref_same,
+                                            "sample": "one component timed (read + serial reorder loop), x 6"},
+                     "load_h5_over_cpu_reference": cpu_s / walls["h5"]}
+        # f1: particles_fields_init.h5
+        fn = os.path.join(work, "particles_fields_init.h5")
+        tp.synth_pic_fields(*[wl.kolmogorov_modes(cfg["nmodes"], cfg["kmin"], cfg["kmax"], a, cfg["seed"] + o)
+                              for a, o in ((cfg["dB"], 0), (cfg["v_rms"], 1000))], 1.0)
+        p = np.ascontiguousarray(p0)
+        ts = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            tp.save_particles_fields(fn, p)
+            ts.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        q = tp.read_particles(fn, len(p))
+        t_rd = time.perf_counter() - t0
+        back = bool(all(np.array_equal(q[k], p[k]) for k in ("x", "y", "z", "qm", "ux", "uy", "uz", "t")))
+        sample = 65536
+        xyzt = np.stack([p["x"][:sample], p["y"][:sample], p["z"][:sample], p["t"][:sample]], 1)
+        d = po.Domain.from_buffer_copy(dom)
+        g = po.Grids.from_buffer_copy(grd)
+        fo = po.make_field(system_type=4, charge_mass=1.0, bc_flag=0, dom=d, grd=g, egrid=he, bgrid=hb)
+        t0 = time.perf_counter()
+        emf_ref = po.get_emf(fo, xyzt)
+        t_emf = (time.perf_counter() - t0) * len(p) / sample
+        fields_same = bool(np.array_equal(emf_ref, tp.get_emf(xyzt)))
+        blob = np.zeros(len(p) * 14, np.float64)
+        t0 = time.perf_counter()
+        blob.tofile(os.path.join(work, "blob"))
+        t_w = time.perf_counter() - t0
+        out["f1"] = {"particles": len(p), "file_mb": os.path.getsize(fn) / 1e6,
+                     "save_s": min(ts), "save_particles_per_s": len(p) / min(ts),
+                     "read_s": t_rd, "read_particles_per_s": len(p) / t_rd, "read_back_identical": back,
+                     "fields_identical_to_oracle_get_emf": fields_same,
+                     "cpu_reference_path": {"s": t_emf + t_w, "particles_per_s": len(p) / (t_emf + t_w), "cores": 1,
+                                            "kind": "port", "sample": "serial get_emf on %d particles scaled to %d, "
+                                            "plus writing the same bytes" % (sample, len(p))},
+                     "save_over_cpu_reference": (t_emf + t_w) / min(ts)}
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    return out
+
+
 def config_bench(name, args):
     """One workload on its own (not the headline line)."""
     import test_particle_gb300 as tp
@@ -868,6 +981,8 @@ def config_bench(name, args):
         out = secondary_bs(tp, wl, cpu=args.cpu_bs)
     elif name == "open":
         out = open_box(tp, wl, args)
+    elif name == "io":
+        out = io_files(tp, wl, args)
     elif name == "gate":
         cfg = wl.config_grid()
         setup_grid(tp, wl, cfg, 0)
@@ -890,7 +1005,7 @@ def main():
     ap.add_argument("--gate-nptl", type=int, default=1 << 26,
                     help="particles of the accuracy gate run (0: skip it)")
     ap.add_argument("--gate-steps", type=int, default=500)
-    ap.add_argument("--config", choices=["abc", "modesum", "surrogate", "bs", "open", "gate"], default=None,
+    ap.add_argument("--config", choices=["abc", "modesum", "surrogate", "bs", "open", "gate", "io"], default=None,
                     help="one workload on its own instead of the headline line")
     ap.add_argument("--nptl", type=int, default=0)
     ap.add_argument("--run-steps", type=int, default=0)

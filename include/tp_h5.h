@@ -80,6 +80,12 @@ int tp_h5_write_poincare(const char *fname, int npoints_total, int ncross, int n
  * float, as its H5Dread with a float memory type does).  One time frame
  * (multi_tframe 0).  Without with_e the E records are zero. */
 int tp_read_pic_fields_h5(const char *fname, const char *gname, int with_e);
+/* The inverse: the device-resident PIC fields (tp_synth_pic_fields,
+ * tp_read_pic_fields_*) written as such a file, group gname (one level),
+ * float datasets cbx, cby, cbz (and ex, ey, ez when with_e) of the records
+ * divided by B0 (E0), reordered to C order on the GPU; exact round trips
+ * through tp_read_pic_fields_h5 when B0 and E0 are powers of two. */
+int tp_save_pic_fields_h5(const char *fname, const char *gname, int with_e);
 
 #ifdef __cplusplus
 }

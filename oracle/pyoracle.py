@@ -221,6 +221,17 @@ def synth_pic_fields(modes_b, modes_v, B0z, nx, ny, nz, nthreads=0):
     return e, b
 
 
+def pic_records_from_c(data, scale, comp, rec):
+    """The reference's reorder of one PIC HDF5 component ([nx][ny][nz] float32)
+    into rec (n x 3 float32, x fastest), in place; returns rec."""
+    d = np.ascontiguousarray(data, dtype=np.float32)
+    nx, ny, nz = d.shape
+    assert rec.dtype == np.float32 and rec.flags.c_contiguous and rec.size == 3 * d.size
+    oracle().or_pic_records_from_c(ptr(d), C.c_long(nx), C.c_long(ny), C.c_long(nz), C.c_double(scale),
+                                   C.c_int(comp), ptr(rec))
+    return rec
+
+
 def get_emf(f, xyzt):
     xyzt = np.ascontiguousarray(xyzt, dtype=np.float64).reshape(-1, 4)
     out = np.zeros((len(xyzt), 6))

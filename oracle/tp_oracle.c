@@ -428,6 +428,15 @@ static void synth_axis(const tp_mode *m, int nm, int axis, int n, int idx, doubl
     }
 }
 
+void or_pic_records_from_c(const float *data, long nx, long ny, long nz, double scale, int comp, float *rec)
+{
+    const long nxy = nx * ny, nyz = ny * nz;
+    for (long i = 0; i != nx; ++i)
+        for (long j = 0; j != ny; ++j)
+            for (long k = 0; k != nz; ++k)
+                rec[3 * (k * nxy + j * nx + i) + comp] = (float)(data[i * nyz + j * nz + k] * scale);
+}
+
 static uint64_t synth_phase0(double phase)
 {
     double rev = phase / (2.0 * M_PI);

@@ -68,6 +68,12 @@ void or_mode_sum(const or_field *f, double x, double y, double z, emfields *emf)
 void or_synth_pic_fields(int nmb, const tp_mode *mb, int nmv, const tp_mode *mv, double B0z,
                          int nx, int ny, int nz, float *e, float *b, int nthreads);
 
+/* One component of a PIC HDF5 field file ([nx][ny][nz] floats, C order) into
+ * the x-fastest {x,y,z} float records, scaled: the reference's reorder loop of
+ * read_pic_bfields_float_h5 / read_pic_efields_float_h5
+ * (src/magnetic_field.c:656-665, src/electric_field.c:474-482), serial. */
+void or_pic_records_from_c(const float *data, long nx, long ny, long nz, double scale, int comp, float *rec);
+
 /* Batch helpers for ctypes callers. */
 void or_get_emf_batch(const or_field *f, int n, const double *xyzt, double *emf6);
 void or_wirz_steps(const or_field *f, int n, particles *p, double dt, int nsteps, int *iescape);

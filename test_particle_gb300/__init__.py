@@ -427,6 +427,14 @@ def read_pic_fields_h5(fname, gname, with_e=True):
           "read_pic_fields_h5")
 
 
+def save_pic_fields_h5(fname, gname, with_e=True):
+    """Write the device-resident PIC fields as the reference's PIC HDF5 file
+    (tp_save_pic_fields_h5): float datasets cbx, cby, cbz (ex, ey, ez) of
+    [nx][ny][nz], the records divided by B0 (E0)."""
+    check(lib().tp_save_pic_fields_h5(str(fname).encode(), str(gname).encode(), C.c_int(1 if with_e else 0)),
+          "save_pic_fields_h5")
+
+
 def h5_info(fname, gname, dset):
     """(dims, type class, type size) of dataset gname/dset (tp_h5_info)."""
     rank, cls, size = C.c_int(), C.c_int(), C.c_int()

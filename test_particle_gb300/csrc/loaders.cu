@@ -11,6 +11,8 @@
 // mixed path's interleaved grid and the single-point functions then use the
 // device copy, and the host arrays stay untouched (tp_fetch_device_fields
 // copies them back when a caller needs them).
+#include <unistd.h>
+
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -120,6 +122,26 @@ __global__ void __launch_bounds__(256) h5_transpose_kernel(const unsigned char* 
         const int kk = k0 + r, i = i0 + threadIdx.x;
         if (i < nx && kk < nz)
             rec[3 * (((size_t)kk * ny + j) * nx + i) + k] = (float)((double)tile[threadIdx.x][r] * scale);
+    }
+}
+
+// The inverse, for writing a PIC field file: record (k * ny + j) * nx + i of
+// component k0 to [i][j][k] of a C-order [nx][ny][nz] float array, divided by
+// the scale (in double, rounded to float).  Tiles of (i, k) at one j as above;
+// block (32, 8), grid (ceil(nx / 32), ceil(nz / 32), ny).
+__global__ void __launch_bounds__(256) h5_untranspose_kernel(const float* __restrict__ rec, int nx, int ny, int nz,
+                                                            double scale, int k0, float* __restrict__ out)
+{
+    __shared__ float tile[32][33];
+    const int i0 = blockIdx.x * 32, kb = blockIdx.y * 32, j = blockIdx.z;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int kk = kb + r, i = i0 + threadIdx.x;
+        if (i < nx && kk < nz) tile[r][threadIdx.x] = rec[3 * (((size_t)kk * ny + j) * nx + i) + k0];
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int i = i0 + r, kk = kb + threadIdx.x;
+        if (i < nx && kk < nz) out[((size_t)i * ny + j) * nz + kk] = (float)((double)tile[threadIdx.x][r] / scale);
     }
 }
 
@@ -305,6 +327,95 @@ extern "C" int tp_read_pic_fields_h5(const char* fname, const char* gname, int w
         set_error(7, "tp_read_pic_fields_h5: %s", e.what());
     } catch (...) {
         set_error(7, "tp_read_pic_fields_h5 failed");
+    }
+    return -1;
+}
+
+// tp_save_pic_fields_h5: the device-resident PIC fields as the reference's
+// PIC HDF5 file (the datasets tp_read_pic_fields_h5 reads), float, the
+// records divided by B0 (E0).  Each component is reordered on the GPU into a
+// C-order array, then streams to the file in whole i-planes through two
+// pinned buffers (the next piece copied while the previous one is written).
+static int save_pic_fields_h5_impl(const char* fname, const char* gname, int with_e)
+{
+    if (!ensure_init()) return -1;
+    const int nx = simul_grid.nx, ny = simul_grid.ny, nz = simul_grid.nz;
+    if (!fname || !gname || nx < 1 || ny < 1 || nz < 1 || ny > 65535 || (nx + 31) / 32 > 65535) {
+        set_error(7, "tp_save_pic_fields_h5: grid %d x %d x %d or no file / group name", nx, ny, nz);
+        return -1;
+    }
+    if (!g.m_bc_f.device_only || !g.m_bc_f.dev || (with_e && (!g.m_ec_f.device_only || !g.m_ec_f.dev))) {
+        set_error(7, "no device-resident PIC fields to save");
+        return -1;
+    }
+    std::string grp = gname;
+    while (!grp.empty() && grp[0] == '/') grp.erase(0, 1);
+    const size_t n = (size_t)nx * ny * nz, plane = (size_t)ny * nz;
+    tph5::Plan plan;
+    tph5::WGroup wg;
+    wg.name = grp;
+    const char* names[6] = {"cbx", "cby", "cbz", "ex", "ey", "ez"};
+    const int ncomp = with_e ? 6 : 3;
+    for (int c = 0; c < ncomp; c++)
+        wg.dsets.push_back({names[c], tph5::Type::ieee(4, false), {(uint64_t)nx, (uint64_t)ny, (uint64_t)nz}});
+    plan.groups.push_back(wg);
+    if (!plan.plan()) {
+        set_error(7, "%s: %s", fname, plan.err.c_str());
+        return -1;
+    }
+    std::string err;
+    int fd = tph5::open_for_write(fname, err);
+    if (fd < 0 || !tph5::write_meta(fd, plan, err)) {
+        if (fd >= 0) close(fd);
+        set_error(7, "%s", err.c_str());
+        return -1;
+    }
+    cudaStream_t s = g.stream;
+    static Scratch out_dev;
+    float* dout = (float*)out_dev.get(sizeof(float) * n);
+    Staging st;
+    const size_t piece_planes = std::max<size_t>(1, std::min<size_t>(nx, kPiece / plane));
+    bool ok = dout != nullptr;
+    for (int b = 0; b < 2 && ok; b++)
+        ok = cuda_ok(cudaMallocHost(&st.host[b], sizeof(float) * plane * piece_planes), "pinned staging") &&
+             cuda_ok(cudaEventCreateWithFlags(&st.done[b], cudaEventDisableTiming), "staging event");
+    for (int c = 0; c < ncomp && ok; c++) {
+        const float* rec = (const float*)(c < 3 ? g.m_bc_f.dev : g.m_ec_f.dev);
+        const dim3 grid((unsigned)((nx + 31) / 32), (unsigned)((nz + 31) / 32), (unsigned)ny), block(32, 8);
+        h5_untranspose_kernel<<<grid, block, 0, s>>>(rec, nx, ny, nz, c < 3 ? B0 : E0, c % 3, dout);
+        ok = cuda_ok(cudaGetLastError(), "field reorder");
+        const tph5::WDataset& d = plan.groups[0].dsets[c];
+        const size_t npieces = ((size_t)nx + piece_planes - 1) / piece_planes;
+        auto enqueue = [&](size_t q) {
+            const size_t i0 = q * piece_planes, m = std::min(piece_planes, (size_t)nx - i0);
+            return cuda_ok(cudaMemcpyAsync(st.host[q & 1], dout + i0 * plane, sizeof(float) * m * plane,
+                                           cudaMemcpyDeviceToHost, s), "field download") &&
+                   cuda_ok(cudaEventRecord(st.done[q & 1], s), "staging event");
+        };
+        if (ok) ok = enqueue(0);
+        for (size_t q = 0; q < npieces && ok; q++) {
+            if (q + 1 < npieces) ok = enqueue(q + 1);  // the next piece copies while this one is written
+            ok = ok && cuda_ok(cudaEventSynchronize(st.done[q & 1]), "staging");
+            const size_t i0 = q * piece_planes, m = std::min(piece_planes, (size_t)nx - i0);
+            if (ok && !tph5::write_elements(fd, d, i0 * plane, m * plane, st.host[q & 1], err)) {
+                set_error(7, "%s: %s", fname, err.c_str());
+                ok = false;
+            }
+        }
+    }
+    ok = cuda_ok(cudaStreamSynchronize(s), "field save") && ok;
+    close(fd);
+    return ok ? 0 : -1;
+}
+
+extern "C" int tp_save_pic_fields_h5(const char* fname, const char* gname, int with_e)
+{
+    try {
+        return save_pic_fields_h5_impl(fname, gname, with_e);
+    } catch (const std::exception& e) {
+        set_error(7, "tp_save_pic_fields_h5: %s", e.what());
+    } catch (...) {
+        set_error(7, "tp_save_pic_fields_h5 failed");
     }
     return -1;
 }

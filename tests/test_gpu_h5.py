@@ -152,3 +152,44 @@ def test_saved_fields_are_the_gpu_get_emf_and_the_oracle(tmp_path):
     for k in ("x", "y", "z", "qm", "ux", "uy", "uz", "t"):
         assert np.array_equal(q[k], p[k][10:]), k
     assert tp.device_status() == 0
+
+
+@pytest.mark.parametrize("scale", [1.0, 0.25])
+def test_saved_pic_file_round_trips(tmp_path, scale):
+    """tp_save_pic_fields_h5 writes the device fields as the reference's PIC
+    file: its datasets are the records reordered to C order and divided by
+    B0 (E0); loading it back gives the same records (B0 and E0 powers of two);
+    the oracle's restatement of the reference's reorder loop gives them too."""
+    import ctypes as C
+    nx, ny, nz = 40, 33, 17
+    dom = tp.Domain()
+    dom.xmax, dom.ymax, dom.zmax = nx - 1.0, ny - 1.0, nz - 1.0
+    grd = tp.Grids()
+    grd.nx, grd.ny, grd.nz, grd.nt = nx, ny, nz, 1
+    grd.dx = grd.dy = grd.dz = 1.0
+    tp.configure(system_type=tp.SYS_PIC, dom=dom, grd=grd)
+    L = tp.lib()
+    L.set_variables_bfield(C.byref(grd), C.byref(dom), C.c_double(scale), C.c_int(0), C.c_int(4))
+    L.set_variables_efield(C.byref(grd), C.byref(dom), C.c_double(scale / 2), C.c_int(0), C.c_int(4))
+    import test_particle_gb300.workloads as wl
+    mb = wl.kolmogorov_modes(64, 1, 6, 0.5, 41)
+    mv = wl.kolmogorov_modes(64, 1, 6, 0.1, 42)
+    tp.synth_pic_fields(mb, mv, 1.0)
+    he, hb = tp.fetch_device_fields()
+    fn = str(tmp_path / "fields_0.h5")
+    tp.save_pic_fields_h5(fn, "/Timestep_0")
+    f = h5ref.File(fn)
+    for c, n in enumerate(NAMES):
+        got = f.read("/Timestep_0/" + n)
+        assert got.dtype == np.dtype("<f4") and got.shape == (nx, ny, nz)
+        rec = (hb if c < 3 else he)[:, c % 3]
+        want = (rec.astype(np.float64) / (scale if c < 3 else scale / 2)).astype(np.float32)
+        assert np.array_equal(got, want.reshape(nz, ny, nx).transpose(2, 1, 0)), n
+        ref = np.zeros((nx * ny * nz, 3), np.float32)
+        po.pic_records_from_c(got, scale if c < 3 else scale / 2, c % 3, ref)
+        assert np.array_equal(ref[:, c % 3], rec), n
+    tp.release_device_fields()
+    tp.read_pic_fields_h5(fn, "Timestep_0")
+    he2, hb2 = tp.fetch_device_fields()
+    assert np.array_equal(he2, he) and np.array_equal(hb2, hb)
+    tp.release_device_fields()
