@@ -764,6 +764,29 @@ def profile_case(prec):
         print(json.dumps({"profile": "train", "train_ms": ms, "ms_per_batch": ms / 16,
                           "train_tflops": flop / (ms * 1e-3) / 1e12}))
         return
+    if prec == "h5":
+        # the PIC HDF5 field file of a 256^3 grid written from and read into
+        # device memory (tp_save_pic_fields_h5, tp_read_pic_fields_h5): the
+        # reorder kernels on 64 MB components
+        import ctypes as C
+        import shutil
+        cfg = wl.config_grid(nptl=1024, steps=1, n=256)
+        dom, grd, _, _, _ = setup_grid(tp, wl, cfg, 0)
+        L = tp.lib()
+        L.set_variables_bfield(C.byref(grd), C.byref(dom), C.c_double(1.0), C.c_int(0), C.c_int(4))
+        L.set_variables_efield(C.byref(grd), C.byref(dom), C.c_double(1.0), C.c_int(0), C.c_int(4))
+        work = tempfile.mkdtemp(prefix="tp_h5prof_")
+        try:
+            fn = os.path.join(work, "fields_0.h5")
+            t0 = time.perf_counter()
+            tp.save_pic_fields_h5(fn, "Timestep_0")
+            t1 = time.perf_counter()
+            tp.read_pic_fields_h5(fn, "Timestep_0")
+            t2 = time.perf_counter()
+        finally:
+            shutil.rmtree(work, ignore_errors=True)
+        print(json.dumps({"profile": "h5", "save_s": t1 - t0, "load_s": t2 - t1}))
+        return
     if prec == "abc":
         tp.check(tp.lib().tp_init(0), "tp_init")
         cfg = wl.config_abc(steps=1000)
@@ -1012,13 +1035,14 @@ def main():
     ap.add_argument("--epochs", type=int, default=16)
     ap.add_argument("--cpu-bs", action="store_true")
     ap.add_argument("--profile", choices=["mixed", "mixed512", "fp64", "fp64fast", "surrogate", "modesum",
-                                          "abc", "train"],
+                                          "abc", "train", "h5"],
                     default=None,
                     help="one tracking launch of a small case for a profiler capture (gridded "
                          "field 256^3, 131072 particles, 200 steps; mixed512: the 512^3 headline field "
                          "and particles, 200 steps; surrogate and modesum: 512-mode field, 155648 "
                          "particles, 20 steps; abc: 65536 particles, 1000 steps; train: one training "
-                         "epoch of the learned field on 1,048,576 samples)")
+                         "epoch of the learned field on 1,048,576 samples; h5: a 256^3 PIC HDF5 field "
+                         "file written and read)")
     args = ap.parse_args()
     if args.profile:
         profile_case(args.profile)

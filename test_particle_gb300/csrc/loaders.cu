@@ -14,6 +14,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <exception>
@@ -127,11 +128,15 @@ __global__ void __launch_bounds__(256) h5_transpose_kernel(const unsigned char* 
 
 // The inverse, for writing a PIC field file: record (k * ny + j) * nx + i of
 // component k0 to [i][j][k] of a C-order [nx][ny][nz] float array, divided by
-// the scale (in double, rounded to float).  Tiles of (i, k) at one j as above;
-// block (32, 8), grid (ceil(nx / 32), ceil(nz / 32), ny).
+// the scale (in double, rounded to float; for a power-of-two scale as a
+// product with its exact reciprocal, the same value without an FP64
+// division).  Tiles of (i, k) at one j as above; block (32, 8), grid
+// (ceil(nx / 32), ceil(nz / 32), ny).
+template <bool POW2>
 __global__ void __launch_bounds__(256) h5_untranspose_kernel(const float* __restrict__ rec, int nx, int ny, int nz,
                                                             double scale, int k0, float* __restrict__ out)
 {
+    const double inv = 1.0 / scale;
     __shared__ float tile[32][33];
     const int i0 = blockIdx.x * 32, kb = blockIdx.y * 32, j = blockIdx.z;
     for (int r = threadIdx.y; r < 32; r += 8) {
@@ -141,7 +146,9 @@ __global__ void __launch_bounds__(256) h5_untranspose_kernel(const float* __rest
     __syncthreads();
     for (int r = threadIdx.y; r < 32; r += 8) {
         const int i = i0 + r, kk = kb + threadIdx.x;
-        if (i < nx && kk < nz) out[((size_t)i * ny + j) * nz + kk] = (float)((double)tile[threadIdx.x][r] / scale);
+        if (i < nx && kk < nz)
+            out[((size_t)i * ny + j) * nz + kk] =
+                (float)(POW2 ? (double)tile[threadIdx.x][r] * inv : (double)tile[threadIdx.x][r] / scale);
     }
 }
 
@@ -382,7 +389,11 @@ static int save_pic_fields_h5_impl(const char* fname, const char* gname, int wit
     for (int c = 0; c < ncomp && ok; c++) {
         const float* rec = (const float*)(c < 3 ? g.m_bc_f.dev : g.m_ec_f.dev);
         const dim3 grid((unsigned)((nx + 31) / 32), (unsigned)((nz + 31) / 32), (unsigned)ny), block(32, 8);
-        h5_untranspose_kernel<<<grid, block, 0, s>>>(rec, nx, ny, nz, c < 3 ? B0 : E0, c % 3, dout);
+        const double scale = c < 3 ? B0 : E0;
+        int ex = 0;
+        const bool pow2 = scale != 0.0 && std::fabs(std::frexp(scale, &ex)) == 0.5 && ex > -1020 && ex < 1020;
+        if (pow2) h5_untranspose_kernel<true><<<grid, block, 0, s>>>(rec, nx, ny, nz, scale, c % 3, dout);
+        else h5_untranspose_kernel<false><<<grid, block, 0, s>>>(rec, nx, ny, nz, scale, c % 3, dout);
         ok = cuda_ok(cudaGetLastError(), "field reorder");
         const tph5::WDataset& d = plan.groups[0].dsets[c];
         const size_t npieces = ((size_t)nx + piece_planes - 1) / piece_planes;
