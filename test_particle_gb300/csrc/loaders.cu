@@ -33,11 +33,16 @@ namespace {
 
 constexpr size_t kPiece = (size_t)16 << 20;  // floats per staging piece (64 MB)
 
-__global__ void scatter_kernel(const float* __restrict__ comp, size_t n, double scale, int k,
-                               float* __restrict__ rec)
+// The three components of a field (comp + k * n) into its {x,y,z} records,
+// scaled: data[i] * B0 into float, as the reference.  Each thread writes a
+// whole 12-byte record, so a warp writes 384 contiguous bytes.
+__global__ void scatter3_kernel(const float* __restrict__ comp, size_t n, double scale, float* __restrict__ rec)
 {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i < n) rec[3 * i + k] = (float)((double)comp[i] * scale);  // data[i] * B0, as the reference
+    if (i < n) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) rec[3 * i + k] = (float)((double)comp[k * n + i] * scale);
+    }
 }
 
 struct Staging {
@@ -82,74 +87,96 @@ bool read_component(const char* fname, size_t n, float* dcomp, Staging& st, cuda
     return ok;
 }
 
-// One raw HDF5 value (ES bytes, big-endian or not) as the float the
+// One raw HDF5 value (es bytes, big-endian or not) as the float the
 // reference's H5Dread with a float memory type gives: doubles rounded to
 // nearest, as a C cast.
-template <int ES, bool BE>
-__device__ __forceinline__ float h5_value(const unsigned char* __restrict__ p)
+__device__ __forceinline__ float h5_value(const unsigned char* __restrict__ p, int es, bool be)
 {
-    if (ES == 4) {
+    if (es == 4) {
         unsigned int w = *(const unsigned int*)p;
-        if (BE) w = __byte_perm(w, 0, 0x0123);
+        if (be) w = __byte_perm(w, 0, 0x0123);
         return __uint_as_float(w);
-    } else {
-        unsigned long long w = *(const unsigned long long*)p;
-        if (BE) {
-            const unsigned int lo = (unsigned int)w, hi = (unsigned int)(w >> 32);
-            w = ((unsigned long long)__byte_perm(lo, 0, 0x0123) << 32) | __byte_perm(hi, 0, 0x0123);
-        }
-        return (float)__longlong_as_double((long long)w);
     }
+    unsigned long long w = *(const unsigned long long*)p;
+    if (be) {
+        const unsigned int lo = (unsigned int)w, hi = (unsigned int)(w >> 32);
+        w = ((unsigned long long)__byte_perm(lo, 0, 0x0123) << 32) | __byte_perm(hi, 0, 0x0123);
+    }
+    return (float)__longlong_as_double((long long)w);
 }
 
-// The reference's C-to-Fortran reorder (src/magnetic_field.c:656-665): the
-// value at [i][j][k] of the file's [nx][ny][nz] array goes to record
-// (k * ny + j) * nx + i, scaled.  32 x 32 tiles of (i, k) at one j through
-// shared memory, so that both the reads (along k) and the writes (along i)
-// are coalesced.  Block (32, 8); grid (ceil(nz / 32), ceil(nx / 32), ny).
-template <int ES, bool BE>
-__global__ void __launch_bounds__(256) h5_transpose_kernel(const unsigned char* __restrict__ raw, int nx,
-                                                          int ny, int nz, double scale, int k,
-                                                          float* __restrict__ rec)
+// The raw components of one field in device memory: component k's
+// [nx][ny][nz] values (es[k] bytes each, big-endian when be[k]) at raw[k].
+struct Raw3 {
+    const unsigned char* raw[3];
+    int es[3];
+    int be[3];
+};
+
+// The reference's C-to-Fortran reorder (src/magnetic_field.c:656-665) of the
+// three components of a field at once: the value at [i][j][k] of each file
+// array goes to record (k * ny + j) * nx + i, scaled.  32 x 32 tiles of
+// (i, k) at one j through shared memory: the reads along k are coalesced and
+// each thread writes a whole 12-byte record, so a warp writes 384 contiguous
+// bytes (no partial sectors).  Block (32, 8); grid (ceil(nz / 32),
+// ceil(nx / 32), ny).
+__global__ void __launch_bounds__(256) h5_transpose3_kernel(Raw3 in, int nx, int ny, int nz, double scale,
+                                                           float* __restrict__ rec)
 {
-    __shared__ float tile[32][33];
+    __shared__ float tile[3][32][33];
     const int k0 = blockIdx.x * 32, i0 = blockIdx.y * 32, j = blockIdx.z;
-    for (int r = threadIdx.y; r < 32; r += 8) {
-        const int i = i0 + r, kk = k0 + threadIdx.x;
-        if (i < nx && kk < nz) tile[r][threadIdx.x] = h5_value<ES, BE>(raw + (((size_t)i * ny + j) * nz + kk) * ES);
-    }
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+        for (int r = threadIdx.y; r < 32; r += 8) {
+            const int i = i0 + r, kk = k0 + threadIdx.x;
+            if (i < nx && kk < nz)
+                tile[c][r][threadIdx.x] =
+                    h5_value(in.raw[c] + (((size_t)i * ny + j) * nz + kk) * in.es[c], in.es[c], in.be[c] != 0);
+        }
     __syncthreads();
     for (int r = threadIdx.y; r < 32; r += 8) {
         const int kk = k0 + r, i = i0 + threadIdx.x;
-        if (i < nx && kk < nz)
-            rec[3 * (((size_t)kk * ny + j) * nx + i) + k] = (float)((double)tile[threadIdx.x][r] * scale);
+        if (i < nx && kk < nz) {
+            float* o = rec + 3 * (((size_t)kk * ny + j) * nx + i);
+#pragma unroll
+            for (int c = 0; c < 3; c++) o[c] = (float)((double)tile[c][threadIdx.x][r] * scale);
+        }
     }
 }
 
-// The inverse, for writing a PIC field file: record (k * ny + j) * nx + i of
-// component k0 to [i][j][k] of a C-order [nx][ny][nz] float array, divided by
-// the scale (in double, rounded to float; for a power-of-two scale as a
-// product with its exact reciprocal, the same value without an FP64
-// division).  Tiles of (i, k) at one j as above; block (32, 8), grid
-// (ceil(nx / 32), ceil(nz / 32), ny).
+// The inverse, for writing a PIC field file: each record (k * ny + j) * nx + i
+// of a field to [i][j][k] of three C-order [nx][ny][nz] float arrays
+// (out + c * n), divided by the scale (in double, rounded to float; for a
+// power-of-two scale as a product with its exact reciprocal, the same value
+// without an FP64 division).  Whole records read (384 contiguous bytes a
+// warp), tiles of (i, k) at one j; block (32, 8), grid (ceil(nx / 32),
+// ceil(nz / 32), ny).
 template <bool POW2>
-__global__ void __launch_bounds__(256) h5_untranspose_kernel(const float* __restrict__ rec, int nx, int ny, int nz,
-                                                            double scale, int k0, float* __restrict__ out)
+__global__ void __launch_bounds__(256) h5_untranspose3_kernel(const float* __restrict__ rec, int nx, int ny, int nz,
+                                                             double scale, float* __restrict__ out)
 {
     const double inv = 1.0 / scale;
-    __shared__ float tile[32][33];
+    const size_t n = (size_t)nx * ny * nz;
+    __shared__ float tile[3][32][33];
     const int i0 = blockIdx.x * 32, kb = blockIdx.y * 32, j = blockIdx.z;
     for (int r = threadIdx.y; r < 32; r += 8) {
         const int kk = kb + r, i = i0 + threadIdx.x;
-        if (i < nx && kk < nz) tile[r][threadIdx.x] = rec[3 * (((size_t)kk * ny + j) * nx + i) + k0];
+        if (i < nx && kk < nz) {
+            const float* q = rec + 3 * (((size_t)kk * ny + j) * nx + i);
+#pragma unroll
+            for (int c = 0; c < 3; c++) tile[c][r][threadIdx.x] = q[c];
+        }
     }
     __syncthreads();
-    for (int r = threadIdx.y; r < 32; r += 8) {
-        const int i = i0 + r, kk = kb + threadIdx.x;
-        if (i < nx && kk < nz)
-            out[((size_t)i * ny + j) * nz + kk] =
-                (float)(POW2 ? (double)tile[threadIdx.x][r] * inv : (double)tile[threadIdx.x][r] / scale);
-    }
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+        for (int r = threadIdx.y; r < 32; r += 8) {
+            const int i = i0 + r, kk = kb + threadIdx.x;
+            if (i < nx && kk < nz) {
+                const double v = (double)tile[c][threadIdx.x][r];
+                out[c * n + ((size_t)i * ny + j) * nz + kk] = (float)(POW2 ? v * inv : v / scale);
+            }
+        }
 }
 
 bool device_records(Mirror& m, size_t bytes)
@@ -188,7 +215,7 @@ extern "C" int tp_read_pic_fields_binary(const char* filepath, int ct)
     cudaStream_t s = g.stream;
     Staging st;
     static Scratch comp;
-    float* dcomp = (float*)comp.get(sizeof(float) * n);
+    float* dcomp = (float*)comp.get(sizeof(float) * 3 * n);
     if (!dcomp) return -1;
     const size_t piece = n < kPiece ? n : kPiece;
     for (int b = 0; b < 2; b++)
@@ -202,13 +229,15 @@ extern "C" int tp_read_pic_fields_binary(const char* filepath, int ct)
     for (int c = 0; c < 6; c++) {
         char fname[4096];
         snprintf(fname, sizeof(fname), "%s%s%d%s", filepath, names[c], ct, ".gda");
-        if (!read_component(fname, n, dcomp, st, s)) {
+        // the component waits in its slot until the field's three are in
+        if (!read_component(fname, n, dcomp + (size_t)(c % 3) * n, st, s)) {
             g.m_bc_f.release();
             g.m_ec_f.release();
             return -1;
         }
+        if (c % 3 != 2) continue;
         float* rec = (float*)(c < 3 ? g.m_bc_f.dev : g.m_ec_f.dev);
-        scatter_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dcomp, n, c < 3 ? B0 : E0, c % 3, rec);
+        scatter3_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dcomp, n, c < 3 ? B0 : E0, rec);
         if (!cuda_ok(cudaGetLastError(), "field scatter")) return -1;
     }
     g.upload_gen++;
@@ -234,8 +263,8 @@ extern "C" int tp_fetch_device_fields(float* host_e, float* host_b)
 // (src/magnetic_field.c:632-692, src/electric_field.c:447-507) into device
 // memory.  Each dataset's [0, nx) x [0, ny) x [0, nz) block streams from the
 // file in whole i-planes through two pinned buffers (reading the next piece
-// while the previous one copies), then one transpose kernel writes the
-// component into the records.
+// while the previous one copies); once a field's three components are on the
+// device, one transpose kernel writes its whole records.
 static int read_pic_fields_h5_impl(const char* fname, const char* gname, int with_e)
 {
     if (!ensure_init()) return -1;
@@ -276,7 +305,7 @@ static int read_pic_fields_h5_impl(const char* fname, const char* gname, int wit
     }
     cudaStream_t s = g.stream;
     static Scratch raw_dev;
-    unsigned char* draw = (unsigned char*)raw_dev.get(es_max * n);
+    unsigned char* draw = (unsigned char*)raw_dev.get(3 * es_max * n);
     if (!draw) return -1;
     const size_t plane = (size_t)ny * nz;
     Staging st;
@@ -294,10 +323,12 @@ static int read_pic_fields_h5_impl(const char* fname, const char* gname, int wit
         return -1;
     };
     if (!with_e && !cuda_ok(cudaMemsetAsync(g.m_ec_f.dev, 0, sizeof(float) * 3 * n, s), "E records")) return fail();
+    Raw3 in;
+    int b = 0;
     for (int c = 0; c < ncomp; c++) {
         const tph5::Dataset& d = ds[c];
         const size_t es = d.type.size;
-        int b = 0;
+        unsigned char* slot = draw + (size_t)(c % 3) * es_max * n;  // waits here until the field's three are in
         for (size_t i0 = 0; i0 < (size_t)nx; i0 += piece_planes) {
             const size_t m = std::min(piece_planes, (size_t)nx - i0);
             if (!cuda_ok(cudaEventSynchronize(st.done[b]), "staging")) return fail();
@@ -306,20 +337,19 @@ static int read_pic_fields_h5_impl(const char* fname, const char* gname, int wit
                 set_error(7, "%s", f.error().c_str());
                 return fail();
             }
-            if (!cuda_ok(cudaMemcpyAsync(draw + i0 * plane * es, st.host[b], m * plane * es, cudaMemcpyHostToDevice, s),
+            if (!cuda_ok(cudaMemcpyAsync(slot + i0 * plane * es, st.host[b], m * plane * es, cudaMemcpyHostToDevice, s),
                          "field upload") ||
                 !cuda_ok(cudaEventRecord(st.done[b], s), "staging event"))
                 return fail();
             b ^= 1;
         }
+        in.raw[c % 3] = slot;
+        in.es[c % 3] = (int)es;
+        in.be[c % 3] = d.type.atom.big_endian ? 1 : 0;
+        if (c % 3 != 2) continue;
         float* rec = (float*)(c < 3 ? g.m_bc_f.dev : g.m_ec_f.dev);
         const dim3 grid((unsigned)((nz + 31) / 32), (unsigned)((nx + 31) / 32), (unsigned)ny), block(32, 8);
-        const double scale = c < 3 ? B0 : E0;
-        const bool be = d.type.atom.big_endian;
-        if (es == 4 && !be) h5_transpose_kernel<4, false><<<grid, block, 0, s>>>(draw, nx, ny, nz, scale, c % 3, rec);
-        else if (es == 4) h5_transpose_kernel<4, true><<<grid, block, 0, s>>>(draw, nx, ny, nz, scale, c % 3, rec);
-        else if (!be) h5_transpose_kernel<8, false><<<grid, block, 0, s>>>(draw, nx, ny, nz, scale, c % 3, rec);
-        else h5_transpose_kernel<8, true><<<grid, block, 0, s>>>(draw, nx, ny, nz, scale, c % 3, rec);
+        h5_transpose3_kernel<<<grid, block, 0, s>>>(in, nx, ny, nz, c < 3 ? B0 : E0, rec);
         if (!cuda_ok(cudaGetLastError(), "field transpose")) return fail();
     }
     g.upload_gen++;
@@ -340,14 +370,15 @@ extern "C" int tp_read_pic_fields_h5(const char* fname, const char* gname, int w
 
 // tp_save_pic_fields_h5: the device-resident PIC fields as the reference's
 // PIC HDF5 file (the datasets tp_read_pic_fields_h5 reads), float, the
-// records divided by B0 (E0).  Each component is reordered on the GPU into a
-// C-order array, then streams to the file in whole i-planes through two
-// pinned buffers (the next piece copied while the previous one is written).
+// records divided by B0 (E0).  Each field's three components are reordered on
+// the GPU into C-order arrays, then each streams to the file in whole
+// i-planes through two pinned buffers (the next piece copied while the
+// previous one is written).
 static int save_pic_fields_h5_impl(const char* fname, const char* gname, int with_e)
 {
     if (!ensure_init()) return -1;
     const int nx = simul_grid.nx, ny = simul_grid.ny, nz = simul_grid.nz;
-    if (!fname || !gname || nx < 1 || ny < 1 || nz < 1 || ny > 65535 || (nx + 31) / 32 > 65535) {
+    if (!fname || !gname || nx < 1 || ny < 1 || nz < 1 || ny > 65535 || (nz + 31) / 32 > 65535) {
         set_error(7, "tp_save_pic_fields_h5: grid %d x %d x %d or no file / group name", nx, ny, nz);
         return -1;
     }
@@ -379,7 +410,7 @@ static int save_pic_fields_h5_impl(const char* fname, const char* gname, int wit
     }
     cudaStream_t s = g.stream;
     static Scratch out_dev;
-    float* dout = (float*)out_dev.get(sizeof(float) * n);
+    float* dout = (float*)out_dev.get(sizeof(float) * 3 * n);
     Staging st;
     const size_t piece_planes = std::max<size_t>(1, std::min<size_t>(nx, kPiece / plane));
     bool ok = dout != nullptr;
@@ -387,19 +418,22 @@ static int save_pic_fields_h5_impl(const char* fname, const char* gname, int wit
         ok = cuda_ok(cudaMallocHost(&st.host[b], sizeof(float) * plane * piece_planes), "pinned staging") &&
              cuda_ok(cudaEventCreateWithFlags(&st.done[b], cudaEventDisableTiming), "staging event");
     for (int c = 0; c < ncomp && ok; c++) {
-        const float* rec = (const float*)(c < 3 ? g.m_bc_f.dev : g.m_ec_f.dev);
-        const dim3 grid((unsigned)((nx + 31) / 32), (unsigned)((nz + 31) / 32), (unsigned)ny), block(32, 8);
-        const double scale = c < 3 ? B0 : E0;
-        int ex = 0;
-        const bool pow2 = scale != 0.0 && std::fabs(std::frexp(scale, &ex)) == 0.5 && ex > -1020 && ex < 1020;
-        if (pow2) h5_untranspose_kernel<true><<<grid, block, 0, s>>>(rec, nx, ny, nz, scale, c % 3, dout);
-        else h5_untranspose_kernel<false><<<grid, block, 0, s>>>(rec, nx, ny, nz, scale, c % 3, dout);
-        ok = cuda_ok(cudaGetLastError(), "field reorder");
+        if (c % 3 == 0) {  // the field's three components, reordered at once
+            const float* rec = (const float*)(c < 3 ? g.m_bc_f.dev : g.m_ec_f.dev);
+            const dim3 grid((unsigned)((nx + 31) / 32), (unsigned)((nz + 31) / 32), (unsigned)ny), block(32, 8);
+            const double scale = c < 3 ? B0 : E0;
+            int ex = 0;
+            const bool pow2 = scale != 0.0 && std::fabs(std::frexp(scale, &ex)) == 0.5 && ex > -1020 && ex < 1020;
+            if (pow2) h5_untranspose3_kernel<true><<<grid, block, 0, s>>>(rec, nx, ny, nz, scale, dout);
+            else h5_untranspose3_kernel<false><<<grid, block, 0, s>>>(rec, nx, ny, nz, scale, dout);
+            ok = cuda_ok(cudaGetLastError(), "field reorder");
+        }
+        const float* src = dout + (size_t)(c % 3) * n;
         const tph5::WDataset& d = plan.groups[0].dsets[c];
         const size_t npieces = ((size_t)nx + piece_planes - 1) / piece_planes;
         auto enqueue = [&](size_t q) {
             const size_t i0 = q * piece_planes, m = std::min(piece_planes, (size_t)nx - i0);
-            return cuda_ok(cudaMemcpyAsync(st.host[q & 1], dout + i0 * plane, sizeof(float) * m * plane,
+            return cuda_ok(cudaMemcpyAsync(st.host[q & 1], src + i0 * plane, sizeof(float) * m * plane,
                                            cudaMemcpyDeviceToHost, s), "field download") &&
                    cuda_ok(cudaEventRecord(st.done[q & 1], s), "staging event");
         };
