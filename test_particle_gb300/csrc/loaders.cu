@@ -36,12 +36,30 @@ constexpr size_t kPiece = (size_t)16 << 20;  // floats per staging piece (64 MB)
 // The three components of a field (comp + k * n) into its {x,y,z} records,
 // scaled: data[i] * B0 into float, as the reference.  Each thread writes a
 // whole 12-byte record, so a warp writes 384 contiguous bytes.
+// With a power-of-two scale the product is exact in double, so one FP32
+// multiply rounds it to the same float without the FP64 pipe (a small
+// fraction of the FP32 rate on this part); other scales take the reference's
+// double product.
+template <bool POW2>
+__device__ __forceinline__ float scaled(float v, double scale)
+{
+    return POW2 ? v * (float)scale : (float)((double)v * scale);
+}
+
+// A power of two (1 included) whose products and reciprocal stay normal.
+inline bool pow2_scale(double scale)
+{
+    int ex = 0;
+    return scale != 0.0 && std::fabs(std::frexp(scale, &ex)) == 0.5 && ex > -100 && ex < 100;
+}
+
+template <bool POW2>
 __global__ void scatter3_kernel(const float* __restrict__ comp, size_t n, double scale, float* __restrict__ rec)
 {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i < n) {
 #pragma unroll
-        for (int k = 0; k < 3; k++) rec[3 * i + k] = (float)((double)comp[k * n + i] * scale);
+        for (int k = 0; k < 3; k++) rec[3 * i + k] = scaled<POW2>(comp[k * n + i], scale);
     }
 }
 
@@ -120,6 +138,7 @@ struct Raw3 {
 // each thread writes a whole 12-byte record, so a warp writes 384 contiguous
 // bytes (no partial sectors).  Block (32, 8); grid (ceil(nz / 32),
 // ceil(nx / 32), ny).
+template <bool POW2>
 __global__ void __launch_bounds__(256) h5_transpose3_kernel(Raw3 in, int nx, int ny, int nz, double scale,
                                                            float* __restrict__ rec)
 {
@@ -139,7 +158,7 @@ __global__ void __launch_bounds__(256) h5_transpose3_kernel(Raw3 in, int nx, int
         if (i < nx && kk < nz) {
             float* o = rec + 3 * (((size_t)kk * ny + j) * nx + i);
 #pragma unroll
-            for (int c = 0; c < 3; c++) o[c] = (float)((double)tile[c][threadIdx.x][r] * scale);
+            for (int c = 0; c < 3; c++) o[c] = scaled<POW2>(tile[c][threadIdx.x][r], scale);
         }
     }
 }
@@ -147,15 +166,15 @@ __global__ void __launch_bounds__(256) h5_transpose3_kernel(Raw3 in, int nx, int
 // The inverse, for writing a PIC field file: each record (k * ny + j) * nx + i
 // of a field to [i][j][k] of three C-order [nx][ny][nz] float arrays
 // (out + c * n), divided by the scale (in double, rounded to float; for a
-// power-of-two scale as a product with its exact reciprocal, the same value
-// without an FP64 division).  Whole records read (384 contiguous bytes a
+// power-of-two scale as an FP32 product with its exact reciprocal, the same
+// value without the FP64 pipe).  Whole records read (384 contiguous bytes a
 // warp), tiles of (i, k) at one j; block (32, 8), grid (ceil(nx / 32),
 // ceil(nz / 32), ny).
 template <bool POW2>
 __global__ void __launch_bounds__(256) h5_untranspose3_kernel(const float* __restrict__ rec, int nx, int ny, int nz,
                                                              double scale, float* __restrict__ out)
 {
-    const double inv = 1.0 / scale;
+    const float inv = (float)(1.0 / scale);
     const size_t n = (size_t)nx * ny * nz;
     __shared__ float tile[3][32][33];
     const int i0 = blockIdx.x * 32, kb = blockIdx.y * 32, j = blockIdx.z;
@@ -173,8 +192,8 @@ __global__ void __launch_bounds__(256) h5_untranspose3_kernel(const float* __res
         for (int r = threadIdx.y; r < 32; r += 8) {
             const int i = i0 + r, kk = kb + threadIdx.x;
             if (i < nx && kk < nz) {
-                const double v = (double)tile[c][threadIdx.x][r];
-                out[c * n + ((size_t)i * ny + j) * nz + kk] = (float)(POW2 ? v * inv : v / scale);
+                const float v = tile[c][threadIdx.x][r];
+                out[c * n + ((size_t)i * ny + j) * nz + kk] = POW2 ? v * inv : (float)((double)v / scale);
             }
         }
 }
@@ -237,7 +256,9 @@ extern "C" int tp_read_pic_fields_binary(const char* filepath, int ct)
         }
         if (c % 3 != 2) continue;
         float* rec = (float*)(c < 3 ? g.m_bc_f.dev : g.m_ec_f.dev);
-        scatter3_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dcomp, n, c < 3 ? B0 : E0, rec);
+        const double scale = c < 3 ? B0 : E0;
+        if (pow2_scale(scale)) scatter3_kernel<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dcomp, n, scale, rec);
+        else scatter3_kernel<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(dcomp, n, scale, rec);
         if (!cuda_ok(cudaGetLastError(), "field scatter")) return -1;
     }
     g.upload_gen++;
@@ -349,7 +370,9 @@ static int read_pic_fields_h5_impl(const char* fname, const char* gname, int wit
         if (c % 3 != 2) continue;
         float* rec = (float*)(c < 3 ? g.m_bc_f.dev : g.m_ec_f.dev);
         const dim3 grid((unsigned)((nz + 31) / 32), (unsigned)((nx + 31) / 32), (unsigned)ny), block(32, 8);
-        h5_transpose3_kernel<<<grid, block, 0, s>>>(in, nx, ny, nz, c < 3 ? B0 : E0, rec);
+        const double scale = c < 3 ? B0 : E0;
+        if (pow2_scale(scale)) h5_transpose3_kernel<true><<<grid, block, 0, s>>>(in, nx, ny, nz, scale, rec);
+        else h5_transpose3_kernel<false><<<grid, block, 0, s>>>(in, nx, ny, nz, scale, rec);
         if (!cuda_ok(cudaGetLastError(), "field transpose")) return fail();
     }
     g.upload_gen++;
@@ -422,9 +445,7 @@ static int save_pic_fields_h5_impl(const char* fname, const char* gname, int wit
             const float* rec = (const float*)(c < 3 ? g.m_bc_f.dev : g.m_ec_f.dev);
             const dim3 grid((unsigned)((nx + 31) / 32), (unsigned)((nz + 31) / 32), (unsigned)ny), block(32, 8);
             const double scale = c < 3 ? B0 : E0;
-            int ex = 0;
-            const bool pow2 = scale != 0.0 && std::fabs(std::frexp(scale, &ex)) == 0.5 && ex > -1020 && ex < 1020;
-            if (pow2) h5_untranspose3_kernel<true><<<grid, block, 0, s>>>(rec, nx, ny, nz, scale, dout);
+            if (pow2_scale(scale)) h5_untranspose3_kernel<true><<<grid, block, 0, s>>>(rec, nx, ny, nz, scale, dout);
             else h5_untranspose3_kernel<false><<<grid, block, 0, s>>>(rec, nx, ny, nz, scale, dout);
             ok = cuda_ok(cudaGetLastError(), "field reorder");
         }

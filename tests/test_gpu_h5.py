@@ -76,9 +76,11 @@ def test_double_files_round_to_float_first(tmp_path):
     tp.release_device_fields()
 
 
-def test_large_grid_streams_in_pieces_b_only(tmp_path):
+@pytest.mark.parametrize("b0", [0.75, 2.0])
+def test_large_grid_streams_in_pieces_b_only(tmp_path, b0):
     """A 320 x 256 x 256 grid (84 MB per component: two staging pieces) and B
-    only: E records zero."""
+    only: E records zero; a power-of-two B0 takes the FP32 product, others the
+    reference's double product, both giving the reference's floats."""
     nx, ny, nz = 320, 256, 256
     dom = tp.Domain()
     dom.xmax, dom.ymax, dom.zmax = nx - 1.0, ny - 1.0, nz - 1.0
@@ -88,7 +90,7 @@ def test_large_grid_streams_in_pieces_b_only(tmp_path):
     tp.configure(system_type=tp.SYS_PIC, dom=dom, grd=grd)
     import ctypes as C
     L = tp.lib()
-    L.set_variables_bfield(C.byref(grd), C.byref(dom), C.c_double(0.75), C.c_int(0), C.c_int(4))
+    L.set_variables_bfield(C.byref(grd), C.byref(dom), C.c_double(b0), C.c_int(0), C.c_int(4))
     rng = np.random.default_rng(12)
     grp = {n: rng.normal(size=(nx, ny, nz)).astype(np.float32) for n in NAMES[:3]}
     fn = str(tmp_path / "big.h5")
@@ -97,7 +99,7 @@ def test_large_grid_streams_in_pieces_b_only(tmp_path):
     he, hb = tp.fetch_device_fields()
     assert not he.any()
     for c, n in enumerate(NAMES[:3]):
-        want = (grp[n].astype(np.float64) * 0.75).astype(np.float32).transpose(2, 1, 0).ravel()
+        want = (grp[n].astype(np.float64) * b0).astype(np.float32).transpose(2, 1, 0).ravel()
         assert np.array_equal(hb[:, c], want), n
     tp.release_device_fields()
 
