@@ -138,7 +138,7 @@ struct Raw3 {
 // each thread writes a whole 12-byte record, so a warp writes 384 contiguous
 // bytes (no partial sectors).  Block (32, 8); grid (ceil(nz / 32),
 // ceil(nx / 32), ny).
-template <bool POW2>
+template <bool POW2, bool F32LE>  // F32LE: every component little-endian float (the usual file)
 __global__ void __launch_bounds__(256) h5_transpose3_kernel(Raw3 in, int nx, int ny, int nz, double scale,
                                                            float* __restrict__ rec)
 {
@@ -148,9 +148,11 @@ __global__ void __launch_bounds__(256) h5_transpose3_kernel(Raw3 in, int nx, int
     for (int c = 0; c < 3; c++)
         for (int r = threadIdx.y; r < 32; r += 8) {
             const int i = i0 + r, kk = k0 + threadIdx.x;
-            if (i < nx && kk < nz)
-                tile[c][r][threadIdx.x] =
-                    h5_value(in.raw[c] + (((size_t)i * ny + j) * nz + kk) * in.es[c], in.es[c], in.be[c] != 0);
+            if (i < nx && kk < nz) {
+                const size_t q = ((size_t)i * ny + j) * nz + kk;
+                tile[c][r][threadIdx.x] = F32LE ? reinterpret_cast<const float*>(in.raw[c])[q]
+                                                : h5_value(in.raw[c] + q * in.es[c], in.es[c], in.be[c] != 0);
+            }
         }
     __syncthreads();
     for (int r = threadIdx.y; r < 32; r += 8) {
@@ -371,8 +373,12 @@ static int read_pic_fields_h5_impl(const char* fname, const char* gname, int wit
         float* rec = (float*)(c < 3 ? g.m_bc_f.dev : g.m_ec_f.dev);
         const dim3 grid((unsigned)((nz + 31) / 32), (unsigned)((nx + 31) / 32), (unsigned)ny), block(32, 8);
         const double scale = c < 3 ? B0 : E0;
-        if (pow2_scale(scale)) h5_transpose3_kernel<true><<<grid, block, 0, s>>>(in, nx, ny, nz, scale, rec);
-        else h5_transpose3_kernel<false><<<grid, block, 0, s>>>(in, nx, ny, nz, scale, rec);
+        const bool p2 = pow2_scale(scale);
+        const bool f32le = in.es[0] == 4 && in.es[1] == 4 && in.es[2] == 4 && !in.be[0] && !in.be[1] && !in.be[2];
+        if (p2 && f32le) h5_transpose3_kernel<true, true><<<grid, block, 0, s>>>(in, nx, ny, nz, scale, rec);
+        else if (p2) h5_transpose3_kernel<true, false><<<grid, block, 0, s>>>(in, nx, ny, nz, scale, rec);
+        else if (f32le) h5_transpose3_kernel<false, true><<<grid, block, 0, s>>>(in, nx, ny, nz, scale, rec);
+        else h5_transpose3_kernel<false, false><<<grid, block, 0, s>>>(in, nx, ny, nz, scale, rec);
         if (!cuda_ok(cudaGetLastError(), "field transpose")) return fail();
     }
     g.upload_gen++;
