@@ -990,6 +990,48 @@ def io_files(tp, wl, args):
     return out
 
 
+def poincare_maps(tp, wl, args):
+    """Poincare maps on the headline's 512^3 gridded B (B0
+    along z): field lines from a 128 x 128 grid of seeds on the plane z = L / 2,
+    RK4 steps of half a cell, 20 crossings of that plane (about 20 box lengths)
+    or 12,288 cells of length each.  The GPU trace of
+    every seed against the oracle's (the reference's next_location loop,
+    pinned bit-exact to it) on every host core for a sample of seeds, the
+    sample compared bit for bit."""
+    cfg = wl.config_grid()
+    dom, grd, _, _, _ = setup_grid(tp, wl, cfg, 0)
+    n = cfg["n"]
+    L = cfg["hi"][0] - cfg["lo"][0]
+    side = args.nptl or 128
+    u = (np.arange(side) + 0.5) / side
+    yy, zz = np.meshgrid(u, u, indexing="ij")
+    seeds = np.stack([yy.ravel() * L, zz.ravel() * L, np.full(side * side, 0.5 * L)], 1)
+    step, ncross, face = 0.5 * cfg["dx"], 20, 2
+    lmax = 12288 * cfg["dx"]
+    tp.poincare_trace(seeds[:256], face, step, lmax, ncross)  # warm-up
+    t0 = time.perf_counter()
+    xo, yo, zo, found = tp.poincare_trace(seeds, face, step, lmax, ncross)
+    t_gpu = time.perf_counter() - t0
+    from oracle import pyoracle as po
+    he, hb = tp.fetch_device_fields()
+    d = po.Domain.from_buffer_copy(dom)
+    g = po.Grids.from_buffer_copy(grd)
+    f = po.make_field(system_type=4, charge_mass=1.0, bc_flag=0, dom=d, grd=g, egrid=he, bgrid=hb)
+    cores = os.cpu_count() or 1
+    sample = np.arange(0, len(seeds), max(1, len(seeds) // (8 * cores)))
+    t0 = time.perf_counter()
+    ref = po.poincare(f, seeds[sample], face, step, lmax, ncross, nthreads=cores)
+    t_cpu = (time.perf_counter() - t0) * len(seeds) / len(sample)
+    same = bool(all(np.array_equal(a[sample], r) for a, r in zip((xo, yo, zo, found), ref)))
+    return {"workload": "poincare_pic_%dcube_%dseeds_%dcrossings" % (n, len(seeds), ncross),
+            "seeds": len(seeds), "step_cells": 0.5, "length_max_cells": 12288, "ncross": ncross,
+            "crossings_found": int(found.sum()), "gpu_s": t_gpu, "seeds_per_s": len(seeds) / t_gpu,
+            "sample_identical_to_oracle": same,
+            "cpu_baseline": {"s": t_cpu, "seeds_per_s": len(seeds) / t_cpu, "cores": cores, "kind": "port",
+                             "sample": "%d of the seeds, scaled" % len(sample)},
+            "gpu_over_cpu": t_cpu / t_gpu}
+
+
 def config_bench(name, args):
     """One workload on its own (not the headline line)."""
     import test_particle_gb300 as tp
@@ -1006,6 +1048,8 @@ def config_bench(name, args):
         out = open_box(tp, wl, args)
     elif name == "io":
         out = io_files(tp, wl, args)
+    elif name == "poincare":
+        out = poincare_maps(tp, wl, args)
     elif name == "gate":
         cfg = wl.config_grid()
         setup_grid(tp, wl, cfg, 0)
@@ -1028,7 +1072,7 @@ def main():
     ap.add_argument("--gate-nptl", type=int, default=1 << 26,
                     help="particles of the accuracy gate run (0: skip it)")
     ap.add_argument("--gate-steps", type=int, default=500)
-    ap.add_argument("--config", choices=["abc", "modesum", "surrogate", "bs", "open", "gate", "io"], default=None,
+    ap.add_argument("--config", choices=["abc", "modesum", "surrogate", "bs", "open", "gate", "io", "poincare"], default=None,
                     help="one workload on its own instead of the headline line")
     ap.add_argument("--nptl", type=int, default=0)
     ap.add_argument("--run-steps", type=int, default=0)
