@@ -583,6 +583,26 @@ def secondary_bs(tp, wl, cpu=True):
     return out
 
 
+def host_buffer(arr, pinned):
+    """A copy of arr in page-locked host memory (a pinned torch buffer viewed
+    as numpy), so that the e2e copies run at the link's rate; pageable if
+    that is not available.  Appends whether it is page-locked to `pinned`."""
+    try:
+        import torch
+        buf = torch.empty(arr.nbytes, dtype=torch.uint8, pin_memory=True)
+        out = buf.numpy().view(arr.dtype).reshape(arr.shape)
+        out[...] = arr
+        host_buffer.keep.append(buf)
+        pinned.append(True)
+        return out
+    except Exception:
+        pinned.append(False)
+        return arr.copy()
+
+
+host_buffer.keep = []
+
+
 def headline(args, world, rank, local, pg):
     import ctypes as C
     import test_particle_gb300 as tp
@@ -634,19 +654,23 @@ def headline(args, world, rank, local, pg):
     d64r = sess.fetch(nt_out, nbins, info.nsdc, particles=False)
     sess.close()
 
-    # ---- e2e: host buffers through the C ABI, copies inside the timed region
+    # ---- e2e: host buffers (page-locked) through the C ABI, copies inside
+    # the timed region
     L = tp.lib()
     nsdc = info.nsdc
-    ptl = p0.copy()
-    esp, ese = np.zeros(nt_out * nbins), np.zeros(nt_out * nbins)
-    dsum, rem = np.zeros(8 * nsdc), np.zeros(nsdc, dtype=np.int32)
-    nst = np.zeros(n, dtype=np.int32)
+    pinned = []
+    p_in = host_buffer(p0, pinned)
+    ptl = host_buffer(p0, pinned)
+    esp, ese = host_buffer(np.zeros(nt_out * nbins), pinned), host_buffer(np.zeros(nt_out * nbins), pinned)
+    dsum, rem = host_buffer(np.zeros(8 * nsdc), pinned), host_buffer(np.zeros(nsdc, dtype=np.int32), pinned)
+    nst = host_buffer(np.zeros(n, dtype=np.int32), pinned)
     ri = tp.RunInfo()
 
     def e2e_once(prec):
+        ptl[...] = p_in  # every run from the workload's initial particles (untimed)
         t1 = time.perf_counter()
         tp.check(L.tp_track_host(C.c_int(prec), C.c_int(n), C.c_double(dt), C.c_int(nt_out),
-                                 C.c_int(nbins), tp._ptr(p0), tp._ptr(ptl), tp._ptr(nst), tp._ptr(esp),
+                                 C.c_int(nbins), tp._ptr(p_in), tp._ptr(ptl), tp._ptr(nst), tp._ptr(esp),
                                  tp._ptr(ese), tp._ptr(dsum), tp._ptr(rem), C.byref(ri)), "e2e")
         return time.perf_counter() - t1
 
@@ -673,7 +697,7 @@ def headline(args, world, rank, local, pg):
             "precision": "FP32 push and field, 64-bit fixed-point positions, FP64 diffusion sums",
             "config": config_dict(cfg),
             "e2e": {"value": pushes * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h, "host_memory": "page-locked" if all(pinned) else "pageable"},
             "gpu_launches": launches,
             "clocks": clocks,
             "roofline": {"bound": "hbm", "achieved": dram_gbs, "peak": hbm, "unit": "GB/s",
