@@ -369,7 +369,15 @@ def secondary_abc(tp, wl):
                 rates[label] = best.pushes / best.kernel_ms * 1e3
     finally:
         sess.close()
-    return {"workload": cfg["name"], "pushes_per_s": rates,
+    pk = compute_peaks(tp)
+    roof = {"flops_per_push": ABC_FLOPS_PER_PUSH,
+            "flops_note": "the reference's push counted on the oracle (90 add, 154 mul, 12 div; sqrt, sin, cos "
+                          "not counted); peaks from the FMA-chain microbenchmark, a multiply-add counting 2",
+            "compute_peaks": pk}
+    for label, peak in (("fp64", "fp64_tflops"), ("fp64fast", "fp64_tflops"), ("mixed", "fp32_tflops")):
+        ach = rates[label] * ABC_FLOPS_PER_PUSH / 1e12
+        roof[label] = {"achieved_tflops": ach, "peak": peak, "frac": ach / pk[peak]}
+    return {"workload": cfg["name"], "pushes_per_s": rates, "roofline": roof,
             "mixed_over_fp64": rates["mixed"] / rates["fp64"],
             "accuracy_vs_fp64": {
                 "particles": n, "steps": cfg["steps"],
@@ -583,6 +591,26 @@ def secondary_bs(tp, wl, cpu=True):
     return out
 
 
+# Floating-point operations of one FP64 Wirz push in the ABC field (90 add/sub,
+# 154 mul, 12 div; 8 sqrt, 8 sin and 8 cos not counted), counted on the
+# oracle's restatement of the reference's push and pinned by
+# tests/test_opcount.py.
+ABC_FLOPS_PER_PUSH = 90 + 154 + 12
+_COMPUTE_PEAKS = {}
+
+
+def compute_peaks(tp):
+    """The CUDA-core FP32, FP64 and packed FP32-pair rates from the library's
+    FMA-chain microbenchmark (MEASURED_PEAKS.json holds HBM and tensor-core
+    figures only), measured once per process."""
+    if not _COMPUTE_PEAKS:
+        for k, v in tp.measure_fma_peaks().items():
+            _COMPUTE_PEAKS[k + "_tflops"] = v / 1e12
+        _COMPUTE_PEAKS["how"] = ("FMA chains, 8 per thread, 32 warps on every SM, CUDA events; a multiply-add "
+                                 "counts 2")
+    return _COMPUTE_PEAKS
+
+
 def host_buffer(arr, pinned):
     """A copy of arr in page-locked host memory (a pinned torch buffer viewed
     as numpy), so that the e2e copies run at the link's rate; pageable if
@@ -700,6 +728,7 @@ def headline(args, world, rank, local, pg):
                     "d2h_bytes_per_step": d2h, "host_memory": "page-locked" if all(pinned) else "pageable"},
             "gpu_launches": launches,
             "clocks": clocks,
+            "compute_peaks": compute_peaks(tp),
             "roofline": {"bound": "hbm", "achieved": dram_gbs, "peak": hbm, "unit": "GB/s",
                          "frac": dram_gbs / hbm, "peak_kind": peak_kind, "traffic": traffic,
                          "kernel": "track_mixed_kernel<PIC>",

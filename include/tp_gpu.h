@@ -298,6 +298,12 @@ int tp_tc_gemm_bf16(int n, int k, const unsigned short *a, const unsigned short 
  * of 16 in [16, 256], k a multiple of 64.  A self-check of the training path. */
 int tp_tc_gemm_train_bf16(int m, int n, int k, const unsigned short *a, const unsigned short *b, float *d);
 
+/* FMA-chain microbenchmark of a CUDA-core pipe: kind 0 FP32, 1 FP64, 2 packed
+ * FP32 pairs (fma.rn.f32x2); *flops = floating-point operations per second
+ * (a multiply-add counts 2), every SM busy, at the clock of the moment.  The
+ * denominators of the compute-bound paths' rooflines. */
+int tp_measure_fma_peak(int kind, double *flops);
+
 /* Field lines of the gridded B (system types 3 and 4) from n seeds [n][3],
  * RK4 steps of length `step` on the unit vector of B, up to length_max in
  * all; xpos/ypos/zpos [n][ncross + 1] get the seed and the first ncross

@@ -399,6 +399,17 @@ def poincare_trace(seeds, face, step, length_max, ncross):
     return xo, yo, zo, found
 
 
+def measure_fma_peaks():
+    """CUDA-core peaks from the library's FMA-chain microbenchmark (FLOP/s):
+    {"fp32": ..., "fp64": ..., "fp32x2": ...}."""
+    out = {}
+    for kind, name in ((0, "fp32"), (1, "fp64"), (2, "fp32x2")):
+        v = C.c_double()
+        check(lib().tp_measure_fma_peak(C.c_int(kind), C.byref(v)), "measure_fma_peak")
+        out[name] = v.value
+    return out
+
+
 def read_pic_fields_binary(filepath, ct):
     """Load <filepath>{bx,by,bz,ex,ey,ez}_<ct>.gda into device memory
     (tp_read_pic_fields_binary), scaled by the B0 / E0 set through

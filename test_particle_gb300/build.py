@@ -39,6 +39,7 @@ UNITS = [
     ("loaders.o", "loaders.cu", []),
     ("h5lite.o", "h5lite.cpp", []),
     ("h5io.o", "h5io.cu", []),
+    ("peaks.o", "peaks.cu", []),
 ]
 
 
