@@ -433,6 +433,15 @@ def secondary_modesum(tp, wl, args):
     finally:
         s.close()
     c3["mixed_over_fp64"] = c3["pushes_per_s"]["mixed"] / c3["pushes_per_s"]["fp64"]
+    pk = compute_peaks(tp)
+    flops = 2 * cfg["nmodes"] * 18  # per push: 2 evaluations x 512 modes x ~18 flops (+ one cosine per mode)
+    c3["roofline"] = {"flops_per_push": flops, "compute_peaks": pk,
+                      "flops_note": "2 evaluations x modes x 18 (the phase, the cosine's argument, 6 amplitude "
+                                    "products and sums); the cosine not counted",
+                      "mixed": {"achieved_tflops": c3["pushes_per_s"]["mixed"] * flops / 1e12,
+                                "frac_fp32": c3["pushes_per_s"]["mixed"] * flops / 1e12 / pk["fp32_tflops"]},
+                      "fp64": {"achieved_tflops": c3["pushes_per_s"]["fp64"] * flops / 1e12,
+                               "frac_fp64": c3["pushes_per_s"]["fp64"] * flops / 1e12 / pk["fp64_tflops"]}}
     acc = {"particles": na, "steps": sa, "frame_steps": [100, 200],
            "spectrum_l1_mixed_per_frame": l1_frames(runs["mixed"]["espect"], runs["fp64"]["espect"]),
            "spectrum_l1_fp64_from_fp32_start_per_frame": l1_frames(runs["fp64_from_fp32_start"]["espect"],
