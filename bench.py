@@ -941,7 +941,7 @@ def open_box(tp, wl, args):
 
 def io_files(tp, wl, args):
     """The field and particle files of the headline workload through the
-    library (SURVEY rows f1, f2): the 512^3 field written as the reference's
+    library: the 512^3 field written as the reference's
     PIC HDF5 file (6 float datasets, 3.2 GB) and as .gda files, read back into
     device memory (records identical to the synthesised ones), against the
     reference's CPU path for the same file (the dataset read, then its serial
@@ -1053,7 +1053,7 @@ def io_files(tp, wl, args):
 
 
 def poincare_maps(tp, wl, args):
-    """Poincare maps on the headline's 512^3 gridded B (B0
+    """Poincare maps (src/poincare_map.c) on the headline's 512^3 gridded B (B0
     along z): field lines from a 128 x 128 grid of seeds on the plane z = L / 2,
     RK4 steps of half a cell, 20 crossings of that plane (about 20 box lengths)
     or 12,288 cells of length each.  The GPU trace of
