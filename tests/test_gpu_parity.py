@@ -193,3 +193,45 @@ def test_track_larger_vs_oracle():
     assert err < 2.5e-9, err  # 10x the measured largest difference (2.5e-10)
     assert np.abs(out["espect"] - ref["espect"]).sum() <= 12
     np.testing.assert_allclose(out["dsum"], ref["dsum"], rtol=1e-6, atol=1e-20)
+
+
+def _extreme(shape, seed):
+    """Float grid values that take every branch of the FP32/FP64 conversions:
+    subnormals, signed zeros, the smallest and largest normals, values whose
+    sums overflow, and ordinary values of every size."""
+    rng = np.random.default_rng(seed)
+    v = (rng.normal(size=shape) * 10.0 ** rng.integers(-45, 39, size=shape)).astype(np.float32)
+    flat = v.reshape(-1)
+    picks = np.array([1e-45, -1e-45, 1e-40, -3e-39, 0.0, -0.0, 1.1754944e-38, -1.1754944e-38, 3.4e38, -3.4e38,
+                      1.0, -1.0], dtype=np.float32)
+    idx = rng.choice(flat.size, size=flat.size // 3, replace=False)
+    flat[idx] = picks[rng.integers(0, len(picks), size=idx.size)]
+    return v
+
+
+@pytest.mark.parametrize("name", ["pic", "pic_mt", "mhd"])
+def test_float_grid_extremes_exact(name):
+    """The FP64 path's float-grid interpolation (its conversions done on the
+    integer bit fields, the rare cases by the conversion instructions) against
+    the oracle bit for bit on grids of extreme values."""
+    s = dict(SC[name])
+    for seed, key in enumerate(("bgrid", "egrid", "vgrid_f")):
+        if s.get(key) is not None:
+            s[key] = _extreme(np.shape(s[key]), seed)
+    for key in ("bgrid_ab", "egrid_ab"):
+        if s.get(key) is not None and s[key][0] is not None:
+            s[key] = tuple(_extreme(np.shape(a), 7 + i) for i, a in enumerate(s[key]))
+    configure(name, **{k: s[k] for k in ("bgrid", "egrid", "vgrid_f", "bgrid_ab", "egrid_ab") if k in s})
+    d = s["dom"]
+    rng = np.random.default_rng(21)
+    n = 20000
+    xyzt = np.zeros((n, 4))
+    xyzt[:, 0] = rng.uniform(d.xmin, d.xmax, n)
+    xyzt[:, 1] = rng.uniform(d.ymin, d.ymax, n)
+    xyzt[:, 2] = rng.uniform(d.zmin, d.zmax, n)
+    xyzt[:, 3] = rng.uniform(0.0, d.tmax, n)
+    out = tp.get_emf(xyzt)
+    ref = po.get_emf(mg.field_from(s), xyzt)
+    assert np.array_equal(out, ref, equal_nan=True)
+    mag = np.abs(out[np.isfinite(out) & (out != 0)])
+    assert (mag > 1e37).any() and (mag < 1e-37).any()  # both ends of the range were taken
