@@ -27,9 +27,14 @@ namespace tp {
 // fields with integer operations, and leave the rare cases (subnormal, zero or
 // out-of-range results, infinities, NaNs) to the conversion instructions.
 //
+#ifndef TP_FP64_CVT_INT
+#define TP_FP64_CVT_INT 1  // 0: the conversion instructions throughout
+#endif
+
 // float -> double: exact for every float.
 __device__ __forceinline__ double f2d_exact(float v)
 {
+    if (!TP_FP64_CVT_INT) return (double)v;
     const uint32_t u = __float_as_uint(v);
     const uint32_t e = (u >> 23) & 0xffu;
     if (e == 0u || e == 0xffu) return (double)v;  // zero, subnormal, infinity, NaN
@@ -41,6 +46,7 @@ __device__ __forceinline__ double f2d_exact(float v)
 // double -> float, rounded to nearest even, as the conversion instruction.
 __device__ __forceinline__ float d2f_rn(double v)
 {
+    if (!TP_FP64_CVT_INT) return (float)v;
     const uint32_t hi = (uint32_t)__double2hiint(v), lo = (uint32_t)__double2loint(v);
     const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;  // the float's exponent field
     if (e < 1 || e > 254) return (float)v;  // zero, subnormal or overflowing results, infinity, NaN
