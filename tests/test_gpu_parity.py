@@ -206,6 +206,10 @@ def _extreme(shape, seed):
                       1.0, -1.0], dtype=np.float32)
     idx = rng.choice(flat.size, size=flat.size // 3, replace=False)
     flat[idx] = picks[rng.integers(0, len(picks), size=idx.size)]
+    # the lower half of the box (nodes are x fastest, z slowest) holds only
+    # subnormal and tiny normal values, so its cells give tiny sums
+    half = flat.size // 2
+    flat[:half] = (rng.normal(size=half) * 10.0 ** rng.integers(-44, -37, size=half)).astype(np.float32)
     return v
 
 
