@@ -20,44 +20,6 @@ namespace tp {
 #define TP_PI 3.14159265358979323846
 #endif
 
-// float <-> double conversions off the FP64 pipe.  On this part a conversion
-// between FP32 and FP64 issues to the FP64 pipe at the rate of an FP64
-// multiply-add, and the reference's float-grid interpolation converts three
-// times per corner and component; these give the same values from the bit
-// fields with integer operations, and leave the rare cases (subnormal, zero or
-// out-of-range results, infinities, NaNs) to the conversion instructions.
-//
-#ifndef TP_FP64_CVT_INT
-#define TP_FP64_CVT_INT 1  // 0: the conversion instructions throughout
-#endif
-
-// float -> double: exact for every float.
-__device__ __forceinline__ double f2d_exact(float v)
-{
-    if (!TP_FP64_CVT_INT) return (double)v;
-    const uint32_t u = __float_as_uint(v);
-    const uint32_t e = (u >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (double)v;  // zero, subnormal, infinity, NaN
-    // exponent rebased from 127 to 1023; the 23 mantissa bits at the top of the 52
-    const uint32_t hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
-    return __hiloint2double((int)hi, (int)(u << 29));
-}
-
-// double -> float, rounded to nearest even, as the conversion instruction.
-__device__ __forceinline__ float d2f_rn(double v)
-{
-    if (!TP_FP64_CVT_INT) return (float)v;
-    const uint32_t hi = (uint32_t)__double2hiint(v), lo = (uint32_t)__double2loint(v);
-    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;  // the float's exponent field
-    if (e < 1 || e > 254) return (float)v;  // zero, subnormal or overflowing results, infinity, NaN
-    // 23 kept mantissa bits: the 20 of the high word and the top 3 of the low word
-    const uint32_t keep = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    const uint32_t drop = lo & 0x1fffffffu, half = 0x10000000u;
-    uint32_t r = ((uint32_t)e << 23) | keep;
-    r += (drop > half || (drop == half && (keep & 1u))) ? 1u : 0u;  // a carry moves into the exponent
-    return __uint_as_float(r | (hi & 0x80000000u));
-}
-
 // get_trilinar_parameters + grid_indices, src/interpolation.c:36-181
 struct Tri64 {
     long c[8];
@@ -184,9 +146,9 @@ __device__ __forceinline__ void interp_f3(const DevField& f, const Tri64& r, con
         for (int i = 0; i < 8; i++) {
             if (!corner_ok(f, r.c[i], status)) continue;
             const float* p = c + 3 * r.c[i];
-            v0 = d2f_rn(f2d_exact(v0) + f2d_exact(__ldg(p + 0)) * r.w[i]);
-            v1 = d2f_rn(f2d_exact(v1) + f2d_exact(__ldg(p + 1)) * r.w[i]);
-            v2 = d2f_rn(f2d_exact(v2) + f2d_exact(__ldg(p + 2)) * r.w[i]);
+            v0 = (float)((double)v0 + (double)__ldg(p + 0) * r.w[i]);
+            v1 = (float)((double)v1 + (double)__ldg(p + 1) * r.w[i]);
+            v2 = (float)((double)v2 + (double)__ldg(p + 2) * r.w[i]);
         }
         out[0] = v0; out[1] = v1; out[2] = v2;
     } else {
@@ -196,12 +158,12 @@ __device__ __forceinline__ void interp_f3(const DevField& f, const Tri64& r, con
             if (!corner_ok(f, r.c[i], status)) continue;
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-                p[k] += f2d_exact(__ldg(a + 3 * r.c[i] + k)) * r.w[i];
-                q[k] += f2d_exact(__ldg(b + 3 * r.c[i] + k)) * r.w[i];
+                p[k] += (double)__ldg(a + 3 * r.c[i] + k) * r.w[i];
+                q[k] += (double)__ldg(b + 3 * r.c[i] + k) * r.w[i];
             }
         }
 #pragma unroll
-        for (int k = 0; k < 3; k++) out[k] = d2f_rn(r.dt * p[k] + (1.0 - r.dt) * q[k]);
+        for (int k = 0; k < 3; k++) out[k] = (float)(r.dt * p[k] + (1.0 - r.dt) * q[k]);
     }
 }
 
@@ -419,11 +381,10 @@ __device__ __forceinline__ void emf64(const DevField& f, double x, double y, dou
         float v[3], b[3];
         interp_f3(f, r, f.vc_f, f.va_f, f.vb_f, v, status);
         interp_f3(f, r, f.bc_f, f.ba_f, f.bb_f, b, status);
-        e[0] = f2d_exact(b[0]); e[1] = f2d_exact(b[1]); e[2] = f2d_exact(b[2]);
-        const double vd[3] = {f2d_exact(v[0]), f2d_exact(v[1]), f2d_exact(v[2])};
-        e[3] = e[1] * vd[2] - e[2] * vd[1];
-        e[4] = e[2] * vd[0] - e[0] * vd[2];
-        e[5] = e[0] * vd[1] - e[1] * vd[0];
+        e[0] = b[0]; e[1] = b[1]; e[2] = b[2];
+        e[3] = e[1] * v[2] - e[2] * v[1];
+        e[4] = e[2] * v[0] - e[0] * v[2];
+        e[5] = e[0] * v[1] - e[1] * v[0];
     } else if (SYS == TP_SYS_PIC) {
         // getemf_pic_test_particle, src/emfields.c:153-166; the reference
         // computes the same corners and weights twice, once is enough
@@ -432,8 +393,8 @@ __device__ __forceinline__ void emf64(const DevField& f, double x, double y, dou
         float ev[3], b[3];
         interp_f3(f, r, f.ec_f, f.ea_f, f.eb_f, ev, status);
         interp_f3(f, r, f.bc_f, f.ba_f, f.bb_f, b, status);
-        e[3] = f2d_exact(ev[0]); e[4] = f2d_exact(ev[1]); e[5] = f2d_exact(ev[2]);
-        e[0] = f2d_exact(b[0]); e[1] = f2d_exact(b[1]); e[2] = f2d_exact(b[2]);
+        e[3] = ev[0]; e[4] = ev[1]; e[5] = ev[2];
+        e[0] = b[0]; e[1] = b[1]; e[2] = b[2];
     } else if (SYS == TP_SYS_MODESUM) {
         uint64_t ux = fixed_frac64((x - f.xmin) / (f.xmax - f.xmin));
         uint64_t uy = fixed_frac64((y - f.ymin) / (f.ymax - f.ymin));

@@ -466,7 +466,7 @@ __device__ __forceinline__ void pm_unit_b(const DevField& f, double x, double y,
     trilinear64(f, x, y, z, 0.0, r);
     float v[3];
     interp_f3(f, r, f.bc_f, f.ba_f, f.bb_f, v, status);
-    double bx = f2d_exact(v[0]), by = f2d_exact(v[1]), bz = f2d_exact(v[2]);
+    double bx = v[0], by = v[1], bz = v[2];
     double ib = 1.0 / sqrt(bx * bx + by * by + bz * bz);
     b[0] = bx * ib;
     b[1] = by * ib;

@@ -215,9 +215,11 @@ def _extreme(shape, seed):
 
 @pytest.mark.parametrize("name", ["pic", "pic_mt", "mhd"])
 def test_float_grid_extremes_exact(name):
-    """The FP64 path's float-grid interpolation (its conversions done on the
-    integer bit fields, the rare cases by the conversion instructions) against
-    the oracle bit for bit on grids of extreme values."""
+    """The FP64 path's float-grid interpolation (each corner's float value and
+    the running float sum widened to double, the product added, the sum
+    rounded back to float, as the reference does) against the oracle bit for
+    bit on grids of extreme values: subnormal sums, signed zeros, values near
+    the top of the float range."""
     s = dict(SC[name])
     for seed, key in enumerate(("bgrid", "egrid", "vgrid_f")):
         if s.get(key) is not None:
