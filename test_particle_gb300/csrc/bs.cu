@@ -350,9 +350,21 @@ __device__ void frame_diagnostics(const DevField& f, const BsArgs& a, int frame,
 // a warp sit at different points of their own steps, but all of them run the
 // field evaluation -- the bulk of the work -- together instead of one path at
 // a time.  The arithmetic and its order are those of bs_step.
+//
+// The extrapolation that ends a midpoint sequence (the tableau, the error
+// norm, the step control with its pow) is the other large block, and each
+// lane reaches it on its own turn.  An FP64 instruction costs the pipe the
+// same time with one active lane as with 32 on this part, so a lane whose
+// sequence is complete holds its last derivative and waits (P_READY) until at
+// least 1/TP_BS_EX_BATCH of the warp's lanes are ready, or every lane is;
+// then the ready lanes extrapolate together.  Waiting changes no particle's
+// arithmetic (0 disables it).
+#ifndef TP_BS_EX_BATCH
+#define TP_BS_EX_BATCH 4
+#endif
 __global__ void __launch_bounds__(128) bs_track_kernel(DevField f, BsArgs a)
 {
-    enum : int { P_INIT, P_MID, P_FINAL };
+    enum : int { P_INIT, P_MID, P_FINAL, P_READY };
     const double STEPFAC1 = 0.65, STEPFAC2 = 0.94, STEPFAC4 = 4.0;
     const double KFAC1 = 0.8, KFAC2 = 0.9;
     const int KMAXX = c_bs.kmaxx;
@@ -368,7 +380,7 @@ __global__ void __launch_bounds__(128) bs_track_kernel(DevField f, BsArgs a)
     int k_targ = 0, k = 0, nrej = 0;
     bool forward = true, clip = false;
     // midpoint
-    double ym[kNv], yn[kNv], hh = 0.0, xnew = 0.0;
+    double ym[kNv], yn[kNv], ydr[kNv], hh = 0.0, xnew = 0.0;
     int nn = 0;
     int phase = P_INIT;
     if (i < a.n) {
@@ -381,11 +393,24 @@ __global__ void __launch_bounds__(128) bs_track_kernel(DevField f, BsArgs a)
     }
     // each turn: one derivs call per lane that still has a particle
     while (i < a.n) {
+        // the extrapolation runs this turn for the lanes ready for it when
+        // enough of the warp's lanes are
+        bool run_ex = true;
+        if (TP_BS_EX_BATCH > 0) {
+            const unsigned act = __activemask();
+            const unsigned rdy = __ballot_sync(act, phase == P_READY);
+            run_ex = __popc(rdy) * TP_BS_EX_BATCH >= __popc(act);
+        }
+        if (phase == P_READY && !run_ex) continue;
         // one call site, so that the lanes of a warp run it together
         double yd[kNv], ye[kNv];
-        for (int q = 0; q < kNv; q++) ye[q] = phase == P_MID ? yn[q] : y[q];
-        const double xe = phase == P_MID ? xnew : phase == P_FINAL ? x + h : x;
-        derivs(f, a.uform, xe, ye, yd, a.status);
+        if (phase == P_READY) {
+            for (int q = 0; q < kNv; q++) yd[q] = ydr[q];
+        } else {
+            for (int q = 0; q < kNv; q++) ye[q] = phase == P_MID ? yn[q] : y[q];
+            const double xe = phase == P_MID ? xnew : phase == P_FINAL ? x + h : x;
+            derivs(f, a.uform, xe, ye, yd, a.status);
+        }
 
         bool begin_step = false;   // set up the next step of this particle
         bool finish = false;       // this particle is done (or failed)
@@ -398,8 +423,8 @@ __global__ void __launch_bounds__(128) bs_track_kernel(DevField f, BsArgs a)
             frame = 0;
             tf = a.t_end * (frame + 1) / a.nt_out;
             begin_step = true;
-        } else if (phase == P_MID) {
-            if (nn + 1 < c_bs.nseq[k]) {  // the next substep of the midpoint
+        } else if (phase == P_MID || phase == P_READY) {
+            if (phase == P_MID && nn + 1 < c_bs.nseq[k]) {  // the next substep of the midpoint
                 const double h2 = 2.0 * hh;
                 for (int q = 0; q < kNv; q++) {
                     double swap = ym[q] + h2 * yd[q];
@@ -410,6 +435,12 @@ __global__ void __launch_bounds__(128) bs_track_kernel(DevField f, BsArgs a)
                 nn++;
                 continue;
             }
+            if (phase == P_MID && !run_ex) {  // the sequence is complete: wait for the others
+                for (int q = 0; q < kNv; q++) ydr[q] = yd[q];
+                phase = P_READY;
+                continue;
+            }
+            phase = P_MID;
             double yseq[kNv];
             for (int q = 0; q < kNv; q++) yseq[q] = 0.5 * (ym[q] + yn[q] + hh * yd[q]);
             // level k of the extrapolation (the loop body of bs_step)
