@@ -356,11 +356,14 @@ __device__ void frame_diagnostics(const DevField& f, const BsArgs& a, int frame,
 // lane reaches it on its own turn.  An FP64 instruction costs the pipe the
 // same time with one active lane as with 32 on this part, so a lane whose
 // sequence is complete holds its last derivative and waits (P_READY) until at
-// least 1/TP_BS_EX_BATCH of the warp's lanes are ready, or every lane is;
-// then the ready lanes extrapolate together.  Waiting changes no particle's
-// arithmetic (0 disables it).
-#ifndef TP_BS_EX_BATCH
-#define TP_BS_EX_BATCH 4
+// least TP_BS_EX_NUM / TP_BS_EX_DEN of the warp's lanes are ready; then the
+// ready lanes extrapolate together.  Waiting changes no particle's arithmetic
+// (TP_BS_EX_NUM 0 disables it).
+#ifndef TP_BS_EX_NUM
+#define TP_BS_EX_NUM 1
+#endif
+#ifndef TP_BS_EX_DEN
+#define TP_BS_EX_DEN 2
 #endif
 __global__ void __launch_bounds__(128) bs_track_kernel(DevField f, BsArgs a)
 {
@@ -396,10 +399,10 @@ __global__ void __launch_bounds__(128) bs_track_kernel(DevField f, BsArgs a)
         // the extrapolation runs this turn for the lanes ready for it when
         // enough of the warp's lanes are
         bool run_ex = true;
-        if (TP_BS_EX_BATCH > 0) {
+        if (TP_BS_EX_NUM > 0) {
             const unsigned act = __activemask();
             const unsigned rdy = __ballot_sync(act, phase == P_READY);
-            run_ex = __popc(rdy) * TP_BS_EX_BATCH >= __popc(act);
+            run_ex = __popc(rdy) * TP_BS_EX_DEN >= __popc(act) * TP_BS_EX_NUM;
         }
         if (phase == P_READY && !run_ex) continue;
         // one call site, so that the lanes of a warp run it together
