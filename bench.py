@@ -574,10 +574,10 @@ def bs_run(tp, wl, n, t_end=0.05, seed=31):
     return y0, y, steps, st, info
 
 
-def secondary_bs(tp, wl, cpu=True):
-    """C5: adaptive Bulirsch-Stoer, 1,048,576 particles in the wire-loop field."""
+def secondary_bs(tp, wl, cpu=True, n=1048576):
+    """C5: adaptive Bulirsch-Stoer, 1,048,576 particles in the wire-loop field
+    (n: a smaller case for a profiler capture)."""
     dom, w = bs_setup(tp)
-    n = 1048576
     y0, y, steps, st, info = bs_run(tp, wl, n)
     out = {"workload": "wire_loop_bs_%dptl" % n,
            "accepted_steps_per_s": info.pushes / info.kernel_ms * 1e3, "kernel_ms": info.kernel_ms,
@@ -1105,7 +1105,7 @@ def config_bench(name, args):
         c3, c4 = secondary_modesum(tp, wl, args)
         out = {"C3_modesum": c3, "C4_surrogate": c4}
     elif name == "bs":
-        out = secondary_bs(tp, wl, cpu=args.cpu_bs)
+        out = secondary_bs(tp, wl, cpu=args.cpu_bs, n=args.nptl or 1048576)
     elif name == "open":
         out = open_box(tp, wl, args)
     elif name == "io":
