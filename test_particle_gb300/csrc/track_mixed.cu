@@ -91,20 +91,12 @@ __device__ __forceinline__ void diff_singles_body(const MixField& f, const PM& p
 // Persistent fixed-step tracking in mixed precision: the same schedule and
 // diagnostics as the FP64 kernel (src/tracking.c:297-462); the mode table of
 // the plane-wave field is staged once per block in shared memory.
-// Bins of the per-frame block histogram kept in shared memory (more bins go
-// straight to the global histogram; frames are rare, so that costs little).
-// The shared memory a block takes is taken from the L1 cache that serves the
-// corner loads.
-#ifndef TP_MIXED_HIST_BINS
-#define TP_MIXED_HIST_BINS kMaxSmemBins
-#endif
-
 template <int SYS>
 __global__ void __launch_bounds__(kBlock, SYS == TP_SYS_PIC ? TP_MIXED_PIC_MINBLOCKS : 4)
     track_mixed_kernel(MixField f, TrackBufs b, TrackParams q)
 {
     __shared__ double red[(kBlock / 32) * 8];
-    __shared__ unsigned int hist[TP_MIXED_HIST_BINS];
+    __shared__ unsigned int hist[kMaxSmemBins];
     __shared__ double dg[DG_ROWS][kBlock];
     extern __shared__ ModePair smodes[];
     if (SYS == TP_SYS_MODESUM) {
@@ -112,7 +104,7 @@ __global__ void __launch_bounds__(kBlock, SYS == TP_SYS_PIC ? TP_MIXED_PIC_MINBL
         __syncthreads();
     }
     const int tx = threadIdx.x;
-    const bool smem_hist = q.nbins <= TP_MIXED_HIST_BINS;
+    const bool smem_hist = q.nbins <= kMaxSmemBins;
     const float dt = (float)q.dt;
     for (int tile = blockIdx.x; tile < q.ntiles; tile += gridDim.x) {
         const int slot = tile * kBlock + tx;
