@@ -343,6 +343,25 @@ def gate_run(tp, wl, cfg, nptl, steps, seed):
     return out
 
 
+def cpu_port_rate(field, dom, cfg, nptl, steps, seed=77):
+    """pushes/s of the oracle (the reference's FP64 fixed-step loop restated,
+    pinned bit-exact to it) on every host core, over a bounded sample of the
+    workload's particles."""
+    from oracle import pyoracle as po
+    import test_particle_gb300.workloads as wl
+    cores = os.cpu_count() or 1
+    d = po.Domain.from_buffer_copy(dom)
+    d.tmax = steps * cfg["dt"] + 0.5 * cfg["dt"]
+    field.dom = d
+    p = wl.shell_particles(nptl, cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"] + seed)
+    t0 = time.perf_counter()
+    po.track_fixed(field, po.spectrum(cfg["nbins"], cfg["emin"], cfg["emax"]), p, cfg["dt"], 1, nthreads=cores)
+    sec = time.perf_counter() - t0
+    return {"value": nptl * steps / sec, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d particles x %d steps (oracle FP64, OpenMP %d threads)" % (nptl, steps, cores),
+            "seconds": sec}
+
+
 def secondary_abc(tp, wl):
     """C1: the ABC force-free field, 65,536 particles x 10,000 steps."""
     cfg = wl.config_abc()
@@ -377,7 +396,11 @@ def secondary_abc(tp, wl):
     for label, peak in (("fp64", "fp64_tflops"), ("fp64fast", "fp64_tflops"), ("mixed", "fp32_tflops")):
         ach = rates[label] * ABC_FLOPS_PER_PUSH / 1e12
         roof[label] = {"achieved_tflops": ach, "peak": peak, "frac": ach / pk[peak]}
-    return {"workload": cfg["name"], "pushes_per_s": rates, "roofline": roof,
+    from oracle import pyoracle as po
+    cpu = cpu_port_rate(po.make_field(system_type=2, charge_mass=1.0, bc_flag=0, abc=(1.0, 1.0, 1.0), B0=1.0,
+                                      lambda0=2 * np.pi), dom, cfg, 65536, 1000)
+    return {"workload": cfg["name"], "pushes_per_s": rates, "roofline": roof, "cpu_baseline": cpu,
+            "mixed_over_cpu": rates["mixed"] / cpu["value"], "fp64_over_cpu": rates["fp64"] / cpu["value"],
             "mixed_over_fp64": rates["mixed"] / rates["fp64"],
             "accuracy_vs_fp64": {
                 "particles": n, "steps": cfg["steps"],
@@ -433,6 +456,10 @@ def secondary_modesum(tp, wl, args):
     finally:
         s.close()
     c3["mixed_over_fp64"] = c3["pushes_per_s"]["mixed"] / c3["pushes_per_s"]["fp64"]
+    from oracle import pyoracle as po
+    c3["cpu_baseline"] = cpu_port_rate(po.make_field(system_type=5, charge_mass=1.0, bc_flag=0, modes=modes,
+                                                     B0=cfg["B0"]), dom, cfg, 4096, 50)
+    c3["mixed_over_cpu"] = c3["pushes_per_s"]["mixed"] / c3["cpu_baseline"]["value"]
     pk = compute_peaks(tp)
     flops = 2 * cfg["nmodes"] * 18  # per push: 2 evaluations x 512 modes x ~18 flops (+ one cosine per mode)
     c3["roofline"] = {"flops_per_push": flops, "compute_peaks": pk,
@@ -458,6 +485,8 @@ def secondary_modesum(tp, wl, args):
         c4["pushes_per_s"]["surrogate"] = rate(16777216, 100, tp.PREC_SURROGATE)[0]
         c4["pushes_per_s"]["fp64_exact_sum"] = c3["pushes_per_s"]["fp64"]
         c4["surrogate_over_fp64"] = c4["pushes_per_s"]["surrogate"] / c3["pushes_per_s"]["fp64"]
+        c4["cpu_baseline"] = dict(c3["cpu_baseline"], note="the exact mode sum on the CPU, as for C3")
+        c4["surrogate_over_cpu"] = c4["pushes_per_s"]["surrogate"] / c3["cpu_baseline"]["value"]
         c4["surrogate_over_mixed_exact_sum"] = c4["pushes_per_s"]["surrogate"] / c3["pushes_per_s"]["mixed"]
         tp.set_tmax(sa * dt + 0.5 * dt)
         s = tp.Session(na)
