@@ -63,6 +63,18 @@ int tp_h5_write_particles_fields(const char *fname, int write_meta, unsigned lon
                                  unsigned long long offset, int nptl, const particles *ptl,
                                  const emfields *emf);
 
+/* trajectory_diagnostics (include/diagnostics.h:53-56, src/diagnostics.c:403-568)
+ * for one process (mpi_size 1), without MPI or libhdf5: sort by final energy,
+ * reload the initial states from data/particles_fields_init.h5, choose
+ * nptl_traj_tot particles from the highest energy down, track them again with
+ * trajectory records every *nsteps_output steps (particle_tracking_hybrid,
+ * traj_diagnose 1) and write data/particle_diagnostics.h5.  Particles of equal
+ * energy keep their array order.  Returns 0, or -1 with tp_last_error() set. */
+int tp_trajectory_diagnostics(int mpi_rank, int mpi_size, int nptl, double dt, double pmass, int nptl_traj_tot,
+                              int system_type, particles *ptl, int *nptl_accumulate, int *nsteps_ptl_tracking,
+                              int nbins, int nt_out, int *nsteps_output, int bc_flag, int tracking_method,
+                              particles *ptl_init);
+
 /* --- data/poincare_map.h5 (src/poincare_map.c:185-235): /poincare_map/{xpos,
  * ypos,zpos} [npoints_total][ncross + 1] native doubles, this rank's rows
  * [nshift, nshift + npoints) (the rank with nshift 0 writes the metadata).

@@ -19,9 +19,12 @@
 #include <fcntl.h>
 #include <unistd.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <exception>
+#include <numeric>
 #include <vector>
 
 #include "../../include/tp_gpu.h"
@@ -345,6 +348,80 @@ static int tp_h5_write_poincare_impl(const char* fname, int npoints_total, int n
     return 0;
 }
 
+// trajectory_diagnostics, src/diagnostics.c:504-568, with
+// sort_particles_energy (:403-437) and init_ptl_traj (:455-481), for one
+// process.  The particles are sorted by energy (gamma - 1 of their final
+// state; particles of equal energy keep their array order, where the
+// reference's quicksort may order them differently), their initial states
+// reloaded from data/particles_fields_init.h5 in that order, and
+// nptl_traj_tot of them chosen at a uniform interval from the highest energy
+// down; they are tracked again with trajectory records every nsteps_output
+// steps (scaled up as the reference does when a particle took more than 1e6
+// steps), and the records are written with their fields to
+// data/particle_diagnostics.h5.  The arrays are updated as the reference
+// updates them (ptl and nsteps_ptl_tracking sorted; nsteps_ptl_tracking then
+// as particle_tracking_hybrid leaves it).
+static int trajectory_diagnostics_impl(int mpi_rank, int mpi_size, int nptl, double dt, double pmass,
+                                       int nptl_traj_tot, int system_type_arg, particles* ptl, int* nptl_accumulate,
+                                       int* nsteps_ptl_tracking, int nbins, int nt_out, int* nsteps_output,
+                                       int bc_flag, int tracking_method, particles* ptl_init)
+{
+    (void)nptl_accumulate;
+    if (mpi_size != 1 || mpi_rank != 0) {
+        set_error(7, "tp_trajectory_diagnostics runs in one process (the reference's own "
+                     "trajectory_diagnostics gathers the ranks' counts over MPI)");
+        return -1;
+    }
+    if (nptl < 1 || nptl_traj_tot < 1 || nptl_traj_tot > nptl || !ptl || !nsteps_ptl_tracking || !nsteps_output ||
+        *nsteps_output < 1 || !ptl_init) {
+        set_error(7, "tp_trajectory_diagnostics: bad arguments");
+        return -1;
+    }
+    // sort_particles_energy
+    std::vector<double> ene((size_t)nptl);
+    for (int i = 0; i < nptl; i++)
+        ene[i] = sqrt(1.0 + ptl[i].ux * ptl[i].ux + ptl[i].uy * ptl[i].uy + ptl[i].uz * ptl[i].uz) - 1.0;
+    std::vector<int> idx((size_t)nptl);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int u, int v) { return ene[u] < ene[v]; });
+    std::vector<particles> init((size_t)nptl);
+    memset(init.data(), 0, sizeof(particles) * (size_t)nptl);
+    char init_name[] = "data/particles_fields_init.h5";
+    if (tp_read_particles(0, nptl, nullptr, init.data(), init_name) != 0) return -1;
+    std::vector<int> nst(nsteps_ptl_tracking, nsteps_ptl_tracking + nptl);
+    for (int i = 0; i < nptl; i++) {
+        ptl[i] = init[idx[i]];
+        nsteps_ptl_tracking[i] = nst[idx[i]];
+    }
+    // init_ptl_traj (one process: particle_broadcast gives it every trajectory particle)
+    const int nptl_traj = nptl_traj_tot;
+    const int interval = nptl / nptl_traj;
+    int ntraj_max = 0;
+    for (int i = 0; i < nptl_traj; i++) ntraj_max = std::max(ntraj_max, nsteps_ptl_tracking[i]);  // as the reference
+    if (ntraj_max > 1.0e6) *nsteps_output = (int)((*nsteps_output) * ((double)ntraj_max) / 1.0e6);
+    std::vector<int> ntraj_accum((size_t)nptl_traj);
+    std::vector<particles> ptl_traj((size_t)nptl_traj);
+    long long ntraj = 0;
+    for (int i = 0, j = nptl - 1; i < nptl_traj; i++, j -= interval) {
+        ntraj_accum[i] = (nsteps_ptl_tracking[j] - 1) / (*nsteps_output) + 1;
+        ntraj += ntraj_accum[i];
+        ptl_traj[i] = ptl[j];
+    }
+    if (ntraj > 2147483647LL) {
+        set_error(7, "tp_trajectory_diagnostics: %lld trajectory points", ntraj);
+        return -1;
+    }
+    for (int i = 1; i < nptl_traj; i++) ntraj_accum[i] += ntraj_accum[i - 1];
+    std::vector<particles> ptl_time((size_t)ntraj);
+    memset(ptl_time.data(), 0, sizeof(particles) * (size_t)ntraj);
+    for (int i = 0; i < nptl_traj; i++) ptl_time[i == 0 ? 0 : ntraj_accum[i - 1]] = ptl_traj[i];
+    particle_tracking_hybrid(0, nptl_traj, dt, nbins, nt_out, bc_flag, *nsteps_output, pmass, ntraj_accum.data(),
+                             tracking_method, 1, ptl_init, nsteps_ptl_tracking, ptl_traj.data(), ptl_time.data());
+    int acc[1] = {(int)ntraj};
+    char out_name[] = "data/particle_diagnostics.h5";
+    return tp_save_particles_fields(0, (int)ntraj, ptl_time.data(), (int)ntraj, acc, out_name, system_type_arg);
+}
+
 extern "C" int tp_h5_read(const char* fname, const char* gname, const char* dset, int rank,
                           const unsigned long long* count, const unsigned long long* offset, int elem_bytes,
                           void* data)
@@ -394,4 +471,16 @@ extern "C" int tp_h5_write_poincare(const char* fname, int npoints_total, int nc
                        return tp_h5_write_poincare_impl(fname, npoints_total, ncross, nshift, npoints, xpos, ypos,
                                                         zpos);
                    });
+}
+
+extern "C" int tp_trajectory_diagnostics(int mpi_rank, int mpi_size, int nptl, double dt, double pmass,
+                                         int nptl_traj_tot, int system_type_arg, particles* ptl, int* nptl_accumulate,
+                                         int* nsteps_ptl_tracking, int nbins, int nt_out, int* nsteps_output,
+                                         int bc_flag, int tracking_method, particles* ptl_init)
+{
+    return guarded("tp_trajectory_diagnostics", [&]() {
+        return trajectory_diagnostics_impl(mpi_rank, mpi_size, nptl, dt, pmass, nptl_traj_tot, system_type_arg, ptl,
+                                           nptl_accumulate, nsteps_ptl_tracking, nbins, nt_out, nsteps_output,
+                                           bc_flag, tracking_method, ptl_init);
+    });
 }
