@@ -52,12 +52,12 @@ extern "C" int tp_poincare_trace(int n, const double* seeds, int face, double st
     int* d_found = nullptr;
     bool ok = cuda_ok(cudaMalloc(&d_seeds, sizeof(double) * 3 * n), "seeds") &&
               cuda_ok(cudaMalloc(&d_out, sizeof(double) * 3 * row), "crossings") &&
-              cuda_ok(cudaMalloc(&d_found, sizeof(int) * (n + 1)), "found");  // + the seed counter
+              cuda_ok(cudaMalloc(&d_found, sizeof(int) * n), "found");
     cudaStream_t s = g.stream;
     if (ok) {
         cudaMemcpyAsync(d_seeds, seeds, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s);
         ok = cuda_ok(fp64::launch_poincare(f, n, d_seeds, face, step, length_max, nc, d_out, d_out + row,
-                                           d_out + 2 * row, d_found, d_found + n, g.d_status, s),
+                                           d_out + 2 * row, d_found, g.d_status, s),
                      "poincare");
     }
     if (ok) {

@@ -26,8 +26,7 @@ namespace tp {
                                     double* out, int* status, cudaStream_t s);                 \
     cudaError_t launch_poincare(const DevField& f, int n, const double* seeds, int face,       \
                                 double h, double lmax, int ncross, double* xo, double* yo,     \
-                                double* zo, int* found, int* next, int* status,                \
-                                cudaStream_t s);                                               \
+                                double* zo, int* found, int* status, cudaStream_t s);          \
     }
 
 TP_DECLARE_FP64_LAUNCHERS(fp64)

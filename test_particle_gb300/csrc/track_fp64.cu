@@ -501,107 +501,50 @@ __device__ __forceinline__ void pm_next(const DevField& f, double& px, double& p
 
 // outputs [n][ncross + 1] per coordinate; entries a seed does not reach keep
 // the reference's fill value 2 * max of the axis
-// One lane per seed at a time, as a state machine whose every turn is one
-// RK4 step at a single call site, the lanes taking new seeds from a counter
-// as theirs finish: an FP64 warp instruction costs this part's FP64 pipe the
-// same time whatever the number of active lanes, so lanes whose field lines
-// are done would otherwise idle while the rest of their warp runs on.  Each
-// seed's steps, crossings and stopping rule are those of the loop
-// of src/poincare_map.c:158-181 (a crossing is the first point with
-// (pre - init) * (pos - init) <= 0; the trace stops after ncross crossings or
-// once the length reaches lmax, at a crossing made on that very step too).
-#ifndef TP_POINCARE_QUEUE
-#define TP_POINCARE_QUEUE 1
-#endif
 __global__ void poincare_kernel(DevField f, int n, const double* __restrict__ seeds, int face, double h,
                                 double lmax, int ncross, double* xo, double* yo, double* zo, int* found,
-                                int* next, int* status)
+                                int* status)
 {
-    int i = atomicAdd(next, 1);
-    double pos[3] = {0.0, 0.0, 0.0}, init = 0.0, length = 0.0;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t row = (size_t)i * (ncross + 1);
+    for (int k = 0; k <= ncross; k++) {
+        xo[row + k] = f.xmax * 2;
+        yo[row + k] = f.ymax * 2;
+        zo[row + k] = f.zmax * 2;
+    }
+    double pos[3] = {seeds[3 * i], seeds[3 * i + 1], seeds[3 * i + 2]};
+    const double init = pos[face];
+    xo[row] = pos[0]; yo[row] = pos[1]; zo[row] = pos[2];
     int icross = 1;
-    size_t row = 0;
-    auto start = [&]() {
-        row = (size_t)i * (ncross + 1);
-        for (int k = 0; k <= ncross; k++) {
-            xo[row + k] = f.xmax * 2;
-            yo[row + k] = f.ymax * 2;
-            zo[row + k] = f.zmax * 2;
-        }
-        pos[0] = seeds[3 * i];
-        pos[1] = seeds[3 * i + 1];
-        pos[2] = seeds[3 * i + 2];
-        init = pos[face];
-        xo[row] = pos[0]; yo[row] = pos[1]; zo[row] = pos[2];
-        icross = 1;
-        length = 0.0;
-    };
-    if (i < n) start();
-#if !TP_POINCARE_QUEUE
-    // one seed per thread (the launch covers every seed): the original loop
-    if (i < n) {
-        while (icross <= ncross) {
-            double cross = 1.0;
-            while (cross > 0 && length < lmax) {
-                double pre = pos[face];
-                pm_next(f, pos[0], pos[1], pos[2], h, status);
-                cross = (pre - init) * (pos[face] - init);
-                length += h;
-            }
-            if (length < lmax) {
-                xo[row + icross] = pos[0];
-                yo[row + icross] = pos[1];
-                zo[row + icross] = pos[2];
-                ++icross;
-            } else {
-                break;
-            }
-        }
-        found[i] = icross - 1;
-    }
-    return;
-#endif
-    while (i < n) {
-        bool done = !(length < lmax);  // no step is taken once the length is reached
-        if (!done) {
-            const double pre = pos[face];
+    double length = 0.0;
+    while (icross <= ncross) {
+        double cross = 1.0;
+        while (cross > 0 && length < lmax) {  // at most lmax / h steps in all
+            double pre = pos[face];
             pm_next(f, pos[0], pos[1], pos[2], h, status);
-            const double cross = (pre - init) * (pos[face] - init);
+            cross = (pre - init) * (pos[face] - init);
             length += h;
-            if (!(cross > 0 && length < lmax)) {
-                if (length < lmax) {  // a crossing
-                    xo[row + icross] = pos[0];
-                    yo[row + icross] = pos[1];
-                    zo[row + icross] = pos[2];
-                    ++icross;
-                    done = icross > ncross;
-                } else {
-                    done = true;
-                }
-            }
         }
-        if (done) {
-            found[i] = icross - 1;
-            i = atomicAdd(next, 1);
-            if (i < n) start();
+        if (length < lmax) {
+            xo[row + icross] = pos[0];
+            yo[row + icross] = pos[1];
+            zo[row + icross] = pos[2];
+            ++icross;
+        } else {
+            break;
         }
     }
+    found[i] = icross - 1;
 }
 
 cudaError_t launch_poincare(const DevField& f, int n, const double* seeds, int face, double h, double lmax,
-                            int ncross, double* xo, double* yo, double* zo, int* found, int* next, int* status,
+                            int ncross, double* xo, double* yo, double* zo, int* found, int* status,
                             cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, poincare_kernel, 128, 0);
-    const int grid = TP_POINCARE_QUEUE ? std::max(1, std::min((n + 127) / 128, sms * std::max(per, 1)))
-                                       : (n + 127) / 128;
-    cudaError_t e = cudaMemsetAsync(next, 0, sizeof(int), s);
-    if (e != cudaSuccess) return e;
-    poincare_kernel<<<grid, 128, 0, s>>>(f, n, seeds, face, h, lmax, ncross, xo, yo, zo, found, next, status);
+    poincare_kernel<<<(n + 127) / 128, 128, 0, s>>>(f, n, seeds, face, h, lmax, ncross, xo, yo, zo, found,
+                                                    status);
     return cudaGetLastError();
 }
 
