@@ -1123,6 +1123,41 @@ def poincare_maps(tp, wl, args):
             "gpu_over_cpu": t_cpu / t_gpu}
 
 
+def fullsize_modesum(tp, wl, args):
+    """C3 and C4 at their configs' own sizes (minutes of GPU time, not in the
+    default line): the exact FP32 mode sum on 4,194,304 particles x 20,000
+    steps and the learned field, trained as in the default line, on
+    16,777,216 particles x 20,000 steps; one run each, device time."""
+    cfg = wl.config_modesum()
+    dom = tp.Domain()
+    dom.xmax = dom.ymax = dom.zmax = 1.0
+    modes = wl.kolmogorov_modes(cfg["nmodes"], cfg["kmin"], cfg["kmax"], cfg["dB"], cfg["seed"], va=cfg["va"])
+    tp.configure(system_type=tp.SYS_MODESUM, dom=dom, modes=modes, mode_B0=cfg["B0"])
+    tp.set_spectrum(cfg["nbins"], cfg["emin"], cfg["emax"])
+    dt, nbins, steps = cfg["dt"], cfg["nbins"], cfg["steps"]
+    out = {}
+
+    def run(n, code, label):
+        tp.set_tmax(steps * dt + 0.5 * dt)
+        p = wl.shell_particles(n, cfg["speed"], cfg["lo"], cfg["hi"], cfg["seed"])
+        s = tp.Session(n)
+        try:
+            s.load(p)
+            info = s.track(dt, cfg["nt_out"], nbins, code)
+            r = s.fetch(cfg["nt_out"], nbins, info.nsdc, particles=False)
+        finally:
+            s.close()
+        out[label] = {"particles": n, "steps": steps, "kernel_s": info.kernel_ms / 1e3,
+                      "pushes_per_s": info.pushes / info.kernel_ms * 1e3, "status": tp.device_status(),
+                      "spectrum_counts_last_frame": float(np.sum(r["espect"][-nbins:]))}
+
+    run(4194304, tp.PREC_MIXED, "C3_mixed_exact_sum")
+    train = train_surrogate(tp, modes, cfg, args)
+    out["C4_train"] = train
+    run(16777216, tp.PREC_SURROGATE, "C4_surrogate")
+    return out
+
+
 def config_bench(name, args):
     """One workload on its own (not the headline line)."""
     import test_particle_gb300 as tp
@@ -1141,6 +1176,8 @@ def config_bench(name, args):
         out = io_files(tp, wl, args)
     elif name == "poincare":
         out = poincare_maps(tp, wl, args)
+    elif name == "fullsize":
+        out = fullsize_modesum(tp, wl, args)
     elif name == "gate":
         cfg = wl.config_grid()
         setup_grid(tp, wl, cfg, 0)
@@ -1163,7 +1200,7 @@ def main():
     ap.add_argument("--gate-nptl", type=int, default=1 << 26,
                     help="particles of the accuracy gate run (0: skip it)")
     ap.add_argument("--gate-steps", type=int, default=500)
-    ap.add_argument("--config", choices=["abc", "modesum", "surrogate", "bs", "open", "gate", "io", "poincare"], default=None,
+    ap.add_argument("--config", choices=["abc", "modesum", "surrogate", "bs", "open", "gate", "io", "poincare", "fullsize"], default=None,
                     help="one workload on its own instead of the headline line")
     ap.add_argument("--nptl", type=int, default=0)
     ap.add_argument("--run-steps", type=int, default=0)
