@@ -1149,7 +1149,7 @@ def fullsize_modesum(tp, wl, args):
             s.close()
         out[label] = {"particles": n, "steps": steps, "kernel_s": info.kernel_ms / 1e3,
                       "pushes_per_s": info.pushes / info.kernel_ms * 1e3, "status": tp.device_status(),
-                      "spectrum_counts_last_frame": float(np.sum(r["espect"][-nbins:]))}
+                      "spectrum_counts_all_frames": float(np.sum(r["espect"]))}  # n x frames when none escape
 
     run(4194304, tp.PREC_MIXED, "C3_mixed_exact_sum")
     train = train_surrogate(tp, modes, cfg, args)
