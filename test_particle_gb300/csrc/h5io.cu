@@ -11,6 +11,9 @@
 //       src/particle_info.c:376-488), the fields at the particles evaluated on
 //       the GPU by the library's FP64 get_emf;
 //   tp_h5_write_particles_fields: the writer alone, with the fields given;
+//   tp_trajectory_diagnostics: the reference's trajectory diagnostics in one
+//       process (src/diagnostics.c:403-568), from particles_fields_init.h5 to
+//       particle_diagnostics.h5;
 //   tp_h5_write_poincare: data/poincare_map.h5 (src/poincare_map.c:185-235).
 // Several ranks writing one file each call with their own records: the file's
 // layout depends only on the totals, so the rank holding the first record
