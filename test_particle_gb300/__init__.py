@@ -490,3 +490,24 @@ def read_particles(fname, n, offset=0):
     check(lib().tp_read_particles(C.c_int(1 if offset else 0), C.c_int(n), _ptr(acc), _ptr(p),
                                   str(fname).encode()), "read_particles")
     return p
+
+
+def trajectory_diagnostics(ptl, nsteps, ptl_init, dt, nptl_traj, nbins, nt_out, nsteps_output, system_type,
+                           bc_flag=0, tracking_method=0, pmass=1.0):
+    """The reference's trajectory diagnostics in one process
+    (tp_trajectory_diagnostics): reads data/particles_fields_init.h5, writes
+    data/particle_diagnostics.h5.  ptl and nsteps (final particles and their
+    step counts) are updated in place as the reference updates them; returns
+    the trajectory output interval actually used."""
+    assert ptl.dtype == PARTICLE_DTYPE and ptl.flags.c_contiguous
+    assert nsteps.dtype == np.int32 and nsteps.flags.c_contiguous
+    init = np.ascontiguousarray(ptl_init, dtype=PARTICLE_DTYPE)
+    every = C.c_int(nsteps_output)
+    L = lib()
+    L.tp_trajectory_diagnostics.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                            C.c_int, C.c_int, C.c_void_p]
+    check(L.tp_trajectory_diagnostics(0, 1, len(ptl), dt, pmass, nptl_traj, system_type, _ptr(ptl), None,
+                                      _ptr(nsteps), nbins, nt_out, C.byref(every), bc_flag, tracking_method,
+                                      _ptr(init)), "trajectory_diagnostics")
+    return every.value
