@@ -442,3 +442,21 @@ def test_unknown_filters_are_refused(lib, tmp_path):
     rc, _ = _read(lib, fn, "/", "d", [0, 0], [4, 6])
     assert rc == -1 and "filter 32001" in _err(lib)
     assert _info(lib, fn, "/", "d")[0] == 0  # the dataset's description still reads
+
+
+def test_trajectory_diagnostics_rejects_what_it_cannot_do(lib):
+    """More than one process (the reference gathers counts over MPI), an empty
+    set or more trajectory particles than particles: errors before any GPU
+    work."""
+    import test_particle_gb300 as tp
+    p = np.zeros(8, dtype=tp.PARTICLE_DTYPE)
+    nst = np.zeros(8, dtype=np.int32)
+    every = C.c_int(4)
+    f = lib.tp_trajectory_diagnostics
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                  C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    for rank, size, n, ntraj in ((0, 2, 8, 2), (1, 1, 8, 2), (0, 1, 0, 1), (0, 1, 8, 9), (0, 1, 8, 0)):
+        assert f(rank, size, n, 0.1, 1.0, ntraj, 4, _ptr(p), None, _ptr(nst), 10, 2, C.byref(every), 0, 0,
+                 _ptr(p)) == -1
+        assert "tp_trajectory_diagnostics" in _err(lib)
+    lib.tp_clear_status()
