@@ -109,13 +109,10 @@ def test_trajectory_diagnostics_file(tmp_path, monkeypatch):
     ptime[np.concatenate([[0], acc[:-1]])] = pt
     nst_exp = nst_sorted.copy()
     _hybrid(L, ntraj_tot, dt, nb, nt, every, acc, 1, p_init.copy(), nst_exp, pt, ptime)
-    # the library's one call
+    # the library's one call, through the Python binding
     p2, nst2, every2 = p.copy(), nst.copy(), C.c_int(every)
-    L.tp_trajectory_diagnostics.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
-                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
-                                            C.c_int, C.c_int, C.c_void_p]
-    assert L.tp_trajectory_diagnostics(0, 1, n, dt, 1.0, ntraj_tot, s["system_type"], _ptr(p2), None, _ptr(nst2),
-                                       nb, nt, C.byref(every2), 0, 0, _ptr(p_init.copy())) == 0
+    assert tp.trajectory_diagnostics(p2, nst2, p_init.copy(), dt, ntraj_tot, nb, nt, every,
+                                     s["system_type"]) == every
     for k in ("x", "y", "z", "qm", "ux", "uy", "uz", "t"):
         assert np.array_equal(p2[k], q[k]), k
     assert np.array_equal(nst2, nst_exp)
