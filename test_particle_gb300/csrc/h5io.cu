@@ -286,8 +286,12 @@ static int tp_read_particles_impl(int mpi_rank, int nptl, int* nptl_accumulate, 
     for (const tph5::Member& m : ds.type.members)
         for (int c = 0; c < 8; c++)
             if (m.name == kPtlNames[c]) {
-                if (m.type.cls < 0 || m.offset + m.type.size > ds.type.size) {
+                if (m.type.cls < 0) {
                     set_error(7, "%s: member %s is not numeric", fname, m.name.c_str());
+                    return -1;
+                }
+                if ((uint64_t)m.offset + m.type.size > ds.type.size) {
+                    set_error(7, "%s: member %s lies outside the record", fname, m.name.c_str());
                     return -1;
                 }
                 mem[c] = &m;

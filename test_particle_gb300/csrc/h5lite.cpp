@@ -574,7 +574,9 @@ bool File::dataset(const char* group, const char* name, Dataset& ds)
         }
     }
     if (!have_space || !have_type || ds.layout < 0) return fail("'%s' is not a dataset", path.c_str());
+    if (ds.layout > 2) return fail("layout class %d: not supported", ds.layout);
     if (ds.type.size == 0 || ds.dims.size() > 32) return fail("bad datatype size or rank");
+    if (ds.layout == 2 && ds.dims.empty()) return fail("chunked layout of a scalar dataset");
     {
         uint64_t n = 1;
         for (uint64_t d : ds.dims) {

@@ -150,6 +150,27 @@ def test_read_particles_takes_any_member_order_and_type(lib, tmp_path):
         assert np.array_equal(q[k][:n], rec[k].astype(np.float64)), k
 
 
+
+def test_read_particles_refuses_a_member_outside_the_record(lib, tmp_path):
+    """A compound member whose offset puts it past the end of the record
+    (here 2^32 - 4: offset + size wraps in 32 bits) is refused before any
+    record is converted."""
+    import struct
+    import test_particle_gb300 as tp
+    dt = np.dtype([("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("qm", "<f8"), ("ux", "<f8"), ("uy", "<f8"),
+                   ("uz", "<f8"), ("t", "<f8")])
+    rec = np.zeros(4, dtype=dt)
+    fn = str(tmp_path / "m.h5")
+    h5ref.write(fn, {"particles_fields": {"particles": rec}}, compound_version=1)
+    b = bytearray(open(fn, "rb").read())
+    at = b.index(b"ux" + b"\0" * 6 + struct.pack("<I", dt.fields["ux"][1])) + 8
+    b[at:at + 4] = struct.pack("<I", 0xFFFFFFFC)
+    open(fn, "wb").write(bytes(b))
+    q = np.zeros(4, dtype=tp.PARTICLE_DTYPE)
+    assert lib.tp_read_particles(0, 4, None, _ptr(q), fn.encode()) == -1
+    assert "member ux lies outside the record" in _err(lib)
+    lib.tp_clear_status()
+
 def _write_ranks(lib, fn, p, emf, counts, order):
     acc = np.cumsum(counts).astype(np.int32)
     starts = np.concatenate([[0], acc[:-1]])
@@ -459,4 +480,34 @@ def test_trajectory_diagnostics_rejects_what_it_cannot_do(lib):
         assert f(rank, size, n, 0.1, 1.0, ntraj, 4, _ptr(p), None, _ptr(nst), 10, 2, C.byref(every), 0, 0,
                  _ptr(p)) == -1
         assert "tp_trajectory_diagnostics" in _err(lib)
+    lib.tp_clear_status()
+
+
+def test_layouts_the_reader_cannot_index_are_refused(lib, tmp_path):
+    """Layout messages that name no storage the reader knows: a version 2
+    message of class 7 (classes are 0 compact, 1 contiguous, 2 chunked), and
+    a chunked layout on a scalar dataspace (a chunk needs a rank).  Both are
+    refused when the dataset is opened."""
+    import struct
+    fn = str(tmp_path / "c.h5")
+    h5ref.write(fn, {"d": np.arange(12.0).reshape(3, 4)}, layout_version=2)
+    b = bytearray(open(fn, "rb").read())
+    at = b.index(bytes([2, 3, 1]) + b"\0" * 5)
+    b[at + 2] = 7
+    open(fn, "wb").write(bytes(b))
+    assert _info(lib, fn, "/", "d")[0] == -1 and "layout class 7" in _err(lib)
+    rc, _ = _read(lib, fn, "/", "d", [0, 0], [3, 4])
+    assert rc == -1 and "layout class 7" in _err(lib)
+    fn = str(tmp_path / "s.h5")
+    h5ref.write(fn, {"s": np.float64(2.5)})
+    assert h5ref.read(fn, "/s") == 2.5
+    b = bytearray(open(fn, "rb").read())
+    addr = h5ref.File(fn).info("/s")[2][1]
+    at = b.index(bytes([3, 1]) + struct.pack("<QQ", addr, 8))
+    # version 3, chunked, dimensionality 1 (the element size only), never written
+    b[at:at + 15] = bytes([3, 2, 1]) + b"\xff" * 8 + struct.pack("<I", 8)
+    open(fn, "wb").write(bytes(b))
+    assert _info(lib, fn, "/", "s")[0] == -1 and "chunked layout of a scalar" in _err(lib)
+    rc, _ = _read(lib, fn, "/", "s", [], [])
+    assert rc == -1 and "chunked layout of a scalar" in _err(lib)
     lib.tp_clear_status()
