@@ -1,6 +1,7 @@
 // session.cu -- device-resident tracking sessions: particle state in HBM as
 // SoA, one persistent tracking launch per run, diagnostics reduced on the GPU.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 
@@ -210,6 +211,11 @@ bool Session::run(const RunSpec& rs, tp_run_info* info)
     if (rs.estep < rs.sstep || rs.einterval < 1 || rs.nt_out < 1) {
         set_error(6, "bad step range: sstep %d estep %d einterval %d nt_out %d", rs.sstep, rs.estep,
                   rs.einterval, rs.nt_out);
+        return false;
+    }
+    // the kernels index the spectra [nt_out][nbins] with 32-bit integers
+    if (rs.nbins < 1 || (long long)rs.nt_out * rs.nbins > INT_MAX) {
+        set_error(6, "spectra of %d frames x %d bins: not supported", rs.nt_out, rs.nbins);
         return false;
     }
     DevField f;

@@ -56,3 +56,23 @@ def test_uniform_field_gyration(prec, tol_u, tol_phase, tol_x):
     zz = p["z"] + p["zshift"]
     np.testing.assert_allclose(zz, p0["z"] + steps * dt * p0["uz"] / gam, rtol=0, atol=tol_x)
     assert tp.device_status() == 0
+
+
+def test_spectra_beyond_32_bit_indexing_are_refused():
+    """A run whose spectra [nt_out][nbins] hold more than 2^31 - 1 entries
+    (the kernels index them with 32-bit integers) is refused before any
+    launch."""
+    dt = 0.01
+    dom = tp.Domain()
+    dom.xmax = dom.ymax = dom.zmax = 1.0
+    dom.tmax = 70000 * dt + 0.5 * dt
+    tp.configure(system_type=tp.SYS_TEST, charge_mass=1.0, bc_flag=0, dom=dom)
+    tp.set_spectrum(40000, 1e-3, 1e2)
+    p0 = np.zeros(4, dtype=tp.PARTICLE_DTYPE)
+    p0["qm"], p0["ux"] = 1.0, 0.1
+    s = tp.Session(4)
+    s.load(p0)
+    with pytest.raises(RuntimeError, match="60000 frames x 40000 bins: not supported"):
+        s.track(dt, 60000, 40000, tp.PREC_MIXED)
+    s.close()
+    tp.lib().tp_clear_status()
