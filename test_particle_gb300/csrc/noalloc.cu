@@ -145,6 +145,8 @@ extern "C" int tp_track_mixed_noalloc(const tp_noalloc_args* a)
         return TP_NOALLOC_EINVAL;
     const int einterval = a->estep / a->nt_out;
     if (einterval < 1) return TP_NOALLOC_EINVAL;
+    // the kernel indexes the spectra [nt_out][nbins] with 32-bit integers
+    if ((long long)a->nt_out * a->nbins > INT_MAX) return TP_NOALLOC_EINVAL;
     if (a->system_type != TP_SYS_FORCEFREE && a->system_type != TP_SYS_PIC) return TP_NOALLOC_EINVAL;
     if (a->system_type == TP_SYS_PIC && (!a->d_grid || a->nx < 2 || a->ny < 2 || a->nz < 2 ||
                                          (unsigned long long)a->nx * a->ny * a->nz >= 0xffffffffull))

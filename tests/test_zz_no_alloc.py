@@ -179,6 +179,9 @@ def test_noalloc_rejects_bad_sizes():
     assert _fn()(C.byref(a)) == ETOOBIG
     a.estep, a.nbins = 100, 5000
     assert _fn()(C.byref(a)) == EINVAL
+    a.estep, a.nt_out, a.nbins = 600_000, 600_000, 4000  # 2.4e9 spectrum entries: past 32-bit indexing
+    assert _fn()(C.byref(a)) == EINVAL
+    a.estep, a.nt_out = 100, 1
     a.nbins, a.system_type = 200, tp.SYS_PIC  # no grid
     assert _fn()(C.byref(a)) == EINVAL
     a.nx = a.ny = a.nz = 2
