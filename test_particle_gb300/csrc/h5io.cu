@@ -27,7 +27,10 @@
 #include <cstdio>
 #include <cstring>
 #include <exception>
+#include <atomic>
+#include <mutex>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "../../include/tp_gpu.h"
@@ -41,6 +44,35 @@ namespace {
 
 const std::vector<std::string> kPtlNames = {"x", "y", "z", "qm", "ux", "uy", "uz", "t"};
 const std::vector<std::string> kEmfNames = {"Bx", "By", "Bz", "Ex", "Ey", "Ez"};
+
+// body(lo, hi) over [0, n) in up to 8 contiguous ranges of at least `grain`
+// items, on threads (the calling thread takes the first range, and the rest
+// when no thread can be started).  body must not throw.
+template <class F>
+void parallel_ranges(size_t n, size_t grain, F body)
+{
+    const size_t nt = std::min<size_t>(8, std::max<size_t>(1, n / std::max<size_t>(grain, 1)));
+    if (nt <= 1) {
+        body((size_t)0, n);
+        return;
+    }
+    const size_t per = (n + nt - 1) / nt;
+    std::vector<std::thread> th;
+    th.reserve(nt);
+    size_t inline_from = n;
+    for (size_t t = 1; t < nt && t * per < n; t++) {
+        const size_t lo = t * per, hi = std::min(n, lo + per);
+        try {
+            th.emplace_back([body, lo, hi]() { body(lo, hi); });
+        } catch (...) {
+            inline_from = lo;
+            break;
+        }
+    }
+    body((size_t)0, std::min(per, n));
+    for (size_t lo = inline_from; lo < n; lo += per) body(lo, std::min(n, lo + per));
+    for (std::thread& t : th) t.join();
+}
 
 // The two datasets of a particles_fields file of ntot records.
 tph5::Plan particles_plan(unsigned long long ntot)
@@ -212,23 +244,40 @@ static int tp_h5_write_particles_fields_impl(const char* fname, int write_meta, 
     }
     const tph5::WDataset* dp = p.find("particles_fields", "particles");
     const tph5::WDataset* de = p.find("particles_fields", "fields");
-    constexpr int kBlock = 65536;
-    std::vector<uint8_t> buf((size_t)kBlock * 64);
-    for (int i0 = 0; i0 < nptl; i0 += kBlock) {
-        const int m = nptl - i0 < kBlock ? nptl - i0 : kBlock;
-        for (int i = 0; i < m; i++) {
-            const particles& q = ptl[i0 + i];
-            const double v[8] = {q.x, q.y, q.z, q.qm, q.ux, q.uy, q.uz, q.t};
-            for (int c = 0; c < 8; c++) tph5::put_f64(&buf[64 * (size_t)i + 8 * c], v[c], true);
+    // ranges of the records on several threads, each converting and writing
+    // blocks of its own (the byte-order conversion and the copies into the
+    // page cache both run at a few GB/s per thread)
+    constexpr size_t kBlock = 65536;
+    std::atomic<bool> failed{false};
+    std::mutex err_lock;
+    parallel_ranges((size_t)nptl, kBlock, [&](size_t lo, size_t hi) {
+        std::string e;
+        try {
+            std::vector<uint8_t> buf(kBlock * 64);
+            for (size_t i0 = lo; i0 < hi && !failed; i0 += kBlock) {
+                const size_t m = std::min(kBlock, hi - i0);
+                for (size_t i = 0; i < m; i++) {
+                    const particles& q = ptl[i0 + i];
+                    const double v[8] = {q.x, q.y, q.z, q.qm, q.ux, q.uy, q.uz, q.t};
+                    for (int c = 0; c < 8; c++) tph5::put_f64(&buf[64 * i + 8 * c], v[c], true);
+                }
+                if (!tph5::write_elements(fd.fd, *dp, offset + i0, m, buf.data(), e)) break;
+                for (size_t i = 0; i < m; i++) {
+                    const emfields& q = emf[i0 + i];
+                    const double v[6] = {q.Bx, q.By, q.Bz, q.Ex, q.Ey, q.Ez};
+                    for (int c = 0; c < 6; c++) tph5::put_f64(&buf[48 * i + 8 * c], v[c], true);
+                }
+                if (!tph5::write_elements(fd.fd, *de, offset + i0, m, buf.data(), e)) break;
+            }
+        } catch (const std::exception& x) {
+            e = x.what();
         }
-        if (!tph5::write_elements(fd.fd, *dp, offset + i0, m, buf.data(), err)) break;
-        for (int i = 0; i < m; i++) {
-            const emfields& q = emf[i0 + i];
-            const double v[6] = {q.Bx, q.By, q.Bz, q.Ex, q.Ey, q.Ez};
-            for (int c = 0; c < 6; c++) tph5::put_f64(&buf[48 * (size_t)i + 8 * c], v[c], true);
+        if (!e.empty()) {
+            std::lock_guard<std::mutex> lk(err_lock);
+            if (err.empty()) err = e;
+            failed = true;
         }
-        if (!tph5::write_elements(fd.fd, *de, offset + i0, m, buf.data(), err)) break;
-    }
+    });
     if (!err.empty()) {
         set_error(7, "%s: %s", fname, err.c_str());
         return -1;
@@ -297,22 +346,27 @@ static int tp_read_particles_impl(int mpi_rank, int nptl, int* nptl_accumulate, 
                 mem[c] = &m;
             }
     const uint64_t off = mpi_rank == 0 ? 0 : (uint64_t)nptl_accumulate[mpi_rank - 1];
-    constexpr uint64_t kBlock = 65536;
-    std::vector<uint8_t> raw(kBlock * ds.type.size);
-    for (uint64_t i0 = 0; i0 < (uint64_t)nptl; i0 += kBlock) {
-        uint64_t m = (uint64_t)nptl - i0 < kBlock ? (uint64_t)nptl - i0 : kBlock;
+    // blocks of about 32 MiB (read on several threads by the reader), each
+    // converted on several threads
+    const uint64_t block = std::max<uint64_t>(65536, ((uint64_t)32 << 20) / ds.type.size);
+    std::vector<uint8_t> raw(std::min<uint64_t>(block, std::max(nptl, 1)) * ds.type.size);
+    for (uint64_t i0 = 0; i0 < (uint64_t)nptl; i0 += block) {
+        uint64_t m = (uint64_t)nptl - i0 < block ? (uint64_t)nptl - i0 : block;
         uint64_t o = off + i0;
         if (!f.read(ds, &o, &m, raw.data())) {
             set_error(7, "%s", f.error().c_str());
             return -1;
         }
-        for (uint64_t i = 0; i < m; i++) {
-            double* rec = (double*)&ptl[i0 + i];
-            const uint8_t* src = &raw[i * ds.type.size];
-            // particles: x, y, z, qm, ux, uy, uz, t are its first eight doubles
-            for (int c = 0; c < 8; c++)
-                if (mem[c]) rec[c] = tph5::decode(mem[c]->type, src + mem[c]->offset);
-        }
+        const size_t es = ds.type.size;
+        parallel_ranges((size_t)m, 65536, [&](size_t lo, size_t hi) {
+            for (size_t i = lo; i < hi; i++) {
+                double* rec = (double*)&ptl[i0 + i];
+                const uint8_t* src = &raw[i * es];
+                // particles: x, y, z, qm, ux, uy, uz, t are its first eight doubles
+                for (int c = 0; c < 8; c++)
+                    if (mem[c]) rec[c] = tph5::decode(mem[c]->type, src + mem[c]->offset);
+            }
+        });
     }
     return 0;
 }

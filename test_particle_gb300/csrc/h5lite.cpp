@@ -11,11 +11,13 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cerrno>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <thread>
 
 namespace tph5 {
 
@@ -29,6 +31,72 @@ uint64_t le(const uint8_t* p, int n)
 }
 
 uint64_t pad8(uint64_t n) { return (n + 7) & ~7ull; }
+
+// pread / pwrite of a whole range, restarted after short transfers and EINTR
+bool pread_all(int fd, uint8_t* d, size_t n, uint64_t at)
+{
+    while (n) {
+        ssize_t r = pread(fd, d, n, (off_t)at);
+        if (r <= 0) {
+            if (r < 0 && errno == EINTR) continue;
+            return false;
+        }
+        d += r;
+        at += (uint64_t)r;
+        n -= (size_t)r;
+    }
+    return true;
+}
+
+bool pwrite_all(int fd, const uint8_t* s, size_t n, uint64_t at)
+{
+    while (n) {
+        ssize_t w = pwrite(fd, s, n, (off_t)at);
+        if (w <= 0) {
+            if (w < 0 && errno == EINTR) continue;
+            return false;
+        }
+        s += w;
+        at += (uint64_t)w;
+        n -= (size_t)w;
+    }
+    return true;
+}
+
+// Transfers of kParallelBytes or more are split into slices of at least
+// 4 MiB over up to kIoThreads threads: one thread copies between the page
+// cache and user memory at a few GB/s, well below the memory's bandwidth.
+// Where no thread can be started, the calling thread does the rest.
+constexpr size_t kParallelBytes = 16u << 20;
+constexpr size_t kIoThreads = 8;
+
+template <class Op>
+bool parallel_io(size_t n, Op op)
+{
+    if (n < kParallelBytes) return op(0, n);
+    const size_t nt = std::min(kIoThreads, n / (4u << 20));
+    const size_t slice = ((n + nt - 1) / nt + 4095) & ~(size_t)4095;
+    std::atomic<bool> ok{true};
+    std::vector<std::thread> th;
+    th.reserve(nt);
+    size_t done_inline = n;  // start of the slices left to this thread
+    for (size_t t = 1; t < nt && t * slice < n; t++) {
+        const size_t a = t * slice, len = std::min(slice, n - a);
+        try {
+            th.emplace_back([&ok, op, a, len]() {
+                if (!op(a, len)) ok = false;
+            });
+        } catch (...) {
+            done_inline = a;
+            break;
+        }
+    }
+    if (!op(0, std::min(slice, n))) ok = false;
+    for (size_t a = done_inline; a < n; a += slice)
+        if (!op(a, std::min(slice, n - a))) ok = false;
+    for (std::thread& t : th) t.join();
+    return ok;
+}
 
 // Bounds-checked cursor over a message body.
 struct Cur {
@@ -312,17 +380,10 @@ bool File::rd(uint64_t addr, void* dst, size_t n)
     if (addr == kUndef || addr + base_ < addr || addr + base_ > size_ || n > size_ - (addr + base_))
         return fail("read of %zu bytes at address %llu beyond the end of the file", n, (unsigned long long)addr);
     uint8_t* d = (uint8_t*)dst;
-    uint64_t at = addr + base_;
-    while (n) {
-        ssize_t r = pread(fd_, d, n, (off_t)at);
-        if (r <= 0) {
-            if (r < 0 && errno == EINTR) continue;
-            return fail("read error at %llu", (unsigned long long)at);
-        }
-        d += r;
-        at += (uint64_t)r;
-        n -= (size_t)r;
-    }
+    const uint64_t at = addr + base_;
+    const int fd = fd_;
+    if (!parallel_io(n, [d, at, fd](size_t a, size_t len) { return pread_all(fd, d + a, len, at + a); }))
+        return fail("read error in %zu bytes at %llu", n, (unsigned long long)at);
     return true;
 }
 
@@ -1032,27 +1093,17 @@ bool Plan::plan()
     return true;
 }
 
+bool read_at(int fd, void* dst, size_t n, uint64_t at)
+{
+    uint8_t* d = (uint8_t*)dst;
+    return parallel_io(n, [fd, d, at](size_t a, size_t len) { return pread_all(fd, d + a, len, at + a); });
+}
+
 int open_for_write(const char* path, std::string& err)
 {
     int fd = ::open(path, O_WRONLY | O_CREAT, 0644);
     if (fd < 0) err = std::string(path) + ": cannot open for writing";
     return fd;
-}
-
-static bool pwrite_all(int fd, const void* p, size_t n, uint64_t at)
-{
-    const uint8_t* s = (const uint8_t*)p;
-    while (n) {
-        ssize_t w = pwrite(fd, s, n, (off_t)at);
-        if (w <= 0) {
-            if (w < 0 && errno == EINTR) continue;
-            return false;
-        }
-        s += w;
-        at += (uint64_t)w;
-        n -= (size_t)w;
-    }
-    return true;
 }
 
 bool write_meta(int fd, const Plan& plan, std::string& err)
@@ -1090,7 +1141,10 @@ bool write_elements(int fd, const WDataset& d, uint64_t first, uint64_t n, const
         err = "records beyond the dataset's extent";
         return false;
     }
-    if (!pwrite_all(fd, bytes, (size_t)(n * d.type.size), d.addr + first * d.type.size)) {
+    const uint8_t* src = (const uint8_t*)bytes;
+    const uint64_t at = d.addr + first * d.type.size;
+    if (!parallel_io((size_t)(n * d.type.size),
+                     [fd, src, at](size_t a, size_t len) { return pwrite_all(fd, src + a, len, at + a); })) {
         err = "write of the records failed";
         return false;
     }

@@ -163,5 +163,8 @@ bool write_meta(int fd, const Plan& plan, std::string& err);
 bool write_elements(int fd, const WDataset& d, uint64_t first, uint64_t n, const void* bytes, std::string& err);
 // Doubles to IEEE binary64 bytes in the given order.
 void put_f64(uint8_t* p, double v, bool big_endian);
+// n bytes at byte `at` of an open file (any file), large ranges on several
+// threads; false on a read error or the end of the file.
+bool read_at(int fd, void* dst, size_t n, uint64_t at);
 
 }  // namespace tph5

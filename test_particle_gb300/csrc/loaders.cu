@@ -11,6 +11,7 @@
 // mixed path's interleaved grid and the single-point functions then use the
 // device copy, and the host arrays stay untouched (tp_fetch_device_fields
 // copies them back when a caller needs them).
+#include <fcntl.h>
 #include <unistd.h>
 
 #include <algorithm>
@@ -75,11 +76,13 @@ struct Staging {
     }
 };
 
-// One component file into dcomp (n floats), double-buffered.
+// One component file into dcomp (n floats), double-buffered; each piece is
+// read on several threads (one thread copies from the page cache at a few
+// GB/s).
 bool read_component(const char* fname, size_t n, float* dcomp, Staging& st, cudaStream_t s)
 {
-    FILE* fp = fopen(fname, "rb");
-    if (!fp) {
+    const int fd = open(fname, O_RDONLY);
+    if (fd < 0) {
         set_error(7, "Unable to open file %s", fname);
         return false;
     }
@@ -90,7 +93,7 @@ bool read_component(const char* fname, size_t n, float* dcomp, Staging& st, cuda
         size_t m = n - done < kPiece ? n - done : kPiece;
         ok = cuda_ok(cudaEventSynchronize(st.done[b]), "staging");  // its previous copy has finished
         if (!ok) break;
-        if (fread(st.host[b], sizeof(float), m, fp) != m) {
+        if (!tph5::read_at(fd, st.host[b], sizeof(float) * m, sizeof(float) * (uint64_t)done)) {
             set_error(7, "file %s holds fewer than %zu values", fname, n);
             ok = false;
             break;
@@ -101,7 +104,7 @@ bool read_component(const char* fname, size_t n, float* dcomp, Staging& st, cuda
         done += m;
         b ^= 1;
     }
-    fclose(fp);
+    close(fd);
     return ok;
 }
 

@@ -95,7 +95,7 @@ def _particles(n, seed):
     return p
 
 
-@pytest.mark.parametrize("n", [0, 1, 70001])
+@pytest.mark.parametrize("n", [0, 1, 70001, 300007])  # the last on several threads
 def test_particles_fields_file_reads_back_exactly(lib, tmp_path, n):
     """The reference's file: /particles_fields/particles [ntot] of
     {x,y,z,qm,ux,uy,uz,t} and /particles_fields/fields [ntot] of
@@ -511,3 +511,24 @@ def test_layouts_the_reader_cannot_index_are_refused(lib, tmp_path):
     rc, _ = _read(lib, fn, "/", "s", [], [])
     assert rc == -1 and "chunked layout of a scalar" in _err(lib)
     lib.tp_clear_status()
+
+
+def test_large_transfers_split_across_threads(lib, tmp_path):
+    """Reads and writes of 16 MiB or more run as slices on several threads:
+    a 24 MB dataset read whole, and 32 MB per coordinate written whole, come
+    back bit for bit (odd sizes, so the last slice is short)."""
+    rng = np.random.default_rng(5)
+    fn = str(tmp_path / "big.h5")
+    v = rng.normal(size=3_000_001)
+    h5ref.write(fn, {"d": v})
+    rc, out = _read(lib, fn, "/", "d", [0], [len(v)])
+    assert rc == 0 and np.array_equal(out, v)
+    rc, out = _read(lib, fn, "/", "d", [17], [2_500_000])
+    assert rc == 0 and np.array_equal(out, v[17:2_500_017])
+    n, nc = 1_000_003, 3
+    xyz = rng.normal(size=(3, n, nc + 1))
+    fn = str(tmp_path / "p.h5")
+    assert lib.tp_h5_write_poincare(fn.encode(), n, nc, 0, n, _ptr(xyz[0]), _ptr(xyz[1]), _ptr(xyz[2])) == 0
+    f = h5ref.File(fn)
+    for name, a in zip(("xpos", "ypos", "zpos"), xyz):
+        assert np.array_equal(f.read("/poincare_map/" + name), a)
