@@ -514,9 +514,9 @@ def test_layouts_the_reader_cannot_index_are_refused(lib, tmp_path):
 
 
 def test_large_transfers_split_across_threads(lib, tmp_path):
-    """Reads and writes of 16 MiB or more run as slices on several threads:
-    a 24 MB dataset read whole, and 32 MB per coordinate written whole, come
-    back bit for bit (odd sizes, so the last slice is short)."""
+    """Reads of 16 MiB or more run as slices on several threads: a 24 MB
+    dataset read whole or from an offset comes back bit for bit (odd sizes, so
+    the last slice is short), and so do 32 MB per coordinate written whole."""
     rng = np.random.default_rng(5)
     fn = str(tmp_path / "big.h5")
     v = rng.normal(size=3_000_001)
