@@ -58,7 +58,6 @@ void parallel_ranges(size_t n, size_t grain, F body)
     }
     const size_t per = (n + nt - 1) / nt;
     std::vector<std::thread> th;
-    th.reserve(nt);
     size_t inline_from = n;
     for (size_t t = 1; t < nt && t * per < n; t++) {
         const size_t lo = t * per, hi = std::min(n, lo + per);

@@ -79,7 +79,6 @@ bool parallel_io(size_t n, Op op)
     const size_t slice = ((n + nt - 1) / nt + 4095) & ~(size_t)4095;
     std::atomic<bool> ok{true};
     std::vector<std::thread> th;
-    th.reserve(nt);
     size_t done_inline = n;  // start of the slices left to this thread
     for (size_t t = 1; t < nt && t * slice < n; t++) {
         const size_t a = t * slice, len = std::min(slice, n - a);
