@@ -66,7 +66,7 @@ bool pwrite_all(int fd, const uint8_t* s, size_t n, uint64_t at)
 // Reads of kParallelBytes or more are split into slices of at least 4 MiB
 // over up to kIoThreads threads: one thread copies from the page cache at a
 // few GB/s, well below the memory's bandwidth (a 3.2 GB field file: 14 GB/s
-// on one thread, 53 GB/s on eight).  Where no thread can be started, the
+// on one thread, 47-53 GB/s on eight).  Where no thread can be started, the
 // calling thread does the rest.
 constexpr size_t kParallelBytes = 16u << 20;
 constexpr size_t kIoThreads = 8;
