@@ -34,6 +34,7 @@ def configure(name, bc_flag=0, **kw):
                  dom=s["dom"], grd=s["grd"], mt=s["mt"],
                  abc=s.get("abc", (1.0, np.sqrt(2 / 3.0), np.sqrt(1 / 3.0))),
                  B0=s.get("B0", 1.0), lambda0=s.get("lambda0", 1.0), vgrid_d=s.get("vgrid_d"),
+                 vgrid_d_ab=s.get("vgrid_d_ab", (None, None)),
                  vgrid_f=s.get("vgrid_f"), bgrid=s.get("bgrid"), egrid=s.get("egrid"),
                  bgrid_ab=s.get("bgrid_ab", (None, None)), egrid_ab=s.get("egrid_ab", (None, None)),
                  wl=s.get("wl"), ibessel=s.get("ibessel", 0))
@@ -241,3 +242,38 @@ def test_float_grid_extremes_exact(name):
     assert np.array_equal(out, ref, equal_nan=True)
     mag = np.abs(out[np.isfinite(out) & (out != 0)])
     assert (mag > 1e37).any() and (mag < 1e-37).any()  # both ends of the range were taken
+
+
+def test_getb_ff_and_gete_ff_by_name():
+    """getb_ff and gete_ff (src/force_free.c:54-86) called by name: B and
+    E = -v x B equal the reference's get_emf at the golden points, and the
+    velocity grid pointers of all three time frames are left as they were
+    (here two distinct frames are set besides the current one)."""
+    import ctypes as C
+
+    class B3(C.Structure):
+        _fields_ = [("Bx", C.c_double), ("By", C.c_double), ("Bz", C.c_double)]
+
+    class E3(C.Structure):
+        _fields_ = [("Ex", C.c_double), ("Ey", C.c_double), ("Ez", C.c_double)]
+
+    emf = load("emf")
+    v = SC["ff_vel"]["vgrid_d"]
+    frames = (np.ascontiguousarray(v * 0.5), np.ascontiguousarray(v * 2.0))
+    configure("ff_vel", vgrid_d_ab=frames)
+    L = tp.lib()
+    names = ("va_double", "vb_double", "vc_double")
+    before = [C.c_void_p.in_dll(L, n).value for n in names]
+    assert before[0] and before[1] and before[0] != before[1]
+    L.getb_ff.restype = None
+    L.gete_ff.restype = None
+    xyzt, want = emf["ff_vel_xyzt"][:16], emf["ff_vel_emf"][:16]
+    got = np.zeros((len(xyzt), 6))
+    for k, (x, y, z, t) in enumerate(xyzt):
+        b, e = B3(), E3()
+        L.getb_ff(C.c_double(x), C.c_double(y), C.c_double(z), C.c_double(t), C.byref(b))
+        L.gete_ff(C.c_double(x), C.c_double(y), C.c_double(z), C.c_double(t), C.byref(b), C.byref(e))
+        got[k] = (b.Bx, b.By, b.Bz, e.Ex, e.Ey, e.Ez)
+    assert [C.c_void_p.in_dll(L, n).value for n in names] == before
+    np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-13 * np.abs(want).max())
+    assert tp.device_status() == 0
