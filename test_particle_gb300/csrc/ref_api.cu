@@ -111,16 +111,14 @@ extern "C" void getemf_ff(double x, double y, double z, double t, struct emfield
 extern "C" void getemf_wlcs(double x, double y, double z, double t, struct emfields* emf)
 { emf_point(TP_SYS_WLCS, x, y, z, t, emf, "getemf_wlcs"); }
 
-// getb_ff: the ABC field alone.  The velocity grids (all three time-frame
-// pointers) are hidden for the one evaluation, so no E is computed, and put
-// back as they were.
+// getb_ff: the ABC field alone.  B does not depend on the velocity grid, so
+// it is the B of the full force-free evaluation; the grid pointers are left
+// alone (clearing them for the call would drop the grids' device copies and
+// make the next call upload them again).
 extern "C" void getb_ff(double x, double y, double z, double t, struct bfields* bmf)
 {
-    vfields_double *sc = vc_double, *sa = va_double, *sb = vb_double;
-    vc_double = nullptr; va_double = nullptr; vb_double = nullptr;
     emfields e;
     emf_point(TP_SYS_FORCEFREE, x, y, z, t, &e, "getb_ff");
-    vc_double = sc; va_double = sa; vb_double = sb;
     bmf->Bx = e.Bx; bmf->By = e.By; bmf->Bz = e.Bz;
 }
 

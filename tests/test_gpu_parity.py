@@ -246,7 +246,7 @@ def test_float_grid_extremes_exact(name):
 
 def test_getb_ff_and_gete_ff_by_name():
     """getb_ff and gete_ff (src/force_free.c:54-86) called by name: B and
-    E = -v x B equal the reference's get_emf at the golden points, and the
+    E = -v x B equal the reference's get_emf at the golden points; the
     velocity grid pointers of all three time frames are left as they were
     (here two distinct frames are set besides the current one)."""
     import ctypes as C
@@ -276,4 +276,5 @@ def test_getb_ff_and_gete_ff_by_name():
         got[k] = (b.Bx, b.By, b.Bz, e.Ex, e.Ey, e.Ez)
     assert [C.c_void_p.in_dll(L, n).value for n in names] == before
     np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-13 * np.abs(want).max())
+
     assert tp.device_status() == 0
