@@ -621,6 +621,7 @@ extern "C" int tp_mlp_train(long long nsamples, int batch, int epochs, double lr
 // forward pass; out: n*6 physical components.
 extern "C" int tp_mlp_eval(int n, const unsigned int* u, float* out)
 {
+    if (n <= 0) return 0;
     if (!M.ready || !mlp_reserve(n < 128 ? 128 : n)) return -1;
     cudaStream_t s = g.stream;
     uint32_t* dU;

@@ -184,6 +184,13 @@ def test_no_gpu_is_an_error_not_a_fallback(lib):
         tp.get_emf(np.zeros((1, 4)))
 
 
+
+def test_empty_learned_field_batch_is_a_no_op(lib):
+    """An empty (or negative) batch of learned-field evaluations returns at
+    once, before any device work or host allocation."""
+    assert lib.tp_mlp_eval(0, None, None) == 0
+    assert lib.tp_mlp_eval(-5, None, None) == 0
+
 @pytest.mark.parametrize("case", ["no_step_label", "no_ff_label", "no_file", "no_wlcs_config"])
 def test_config_errors_exit_like_the_reference(tmp_path, case):
     """Malformed or missing configuration: a message on stdout and exit(1), as
