@@ -34,7 +34,9 @@ extern "C" int tp_poincare_trace(int n, const double* seeds, int face, double st
                   system_type);
         return -1;
     }
-    if (n < 0 || face < 0 || face > 2 || !(step > 0.0) || !(length_max > 0.0) || nc < 1 ||
+    // (crossings per seed up to 2^24: the rows of nc + 1 entries are indexed
+    // with 32-bit counts)
+    if (n < 0 || face < 0 || face > 2 || !(step > 0.0) || !(length_max > 0.0) || nc < 1 || nc > (1 << 24) ||
         length_max / step > 2147483647.0) {
         set_error(6, "bad Poincare map arguments: n %d face %d step %g length %g crossings %d", n, face,
                   step, length_max, nc);

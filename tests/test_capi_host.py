@@ -191,6 +191,29 @@ def test_empty_learned_field_batch_is_a_no_op(lib):
     assert lib.tp_mlp_eval(0, None, None) == 0
     assert lib.tp_mlp_eval(-5, None, None) == 0
 
+
+def test_poincare_arguments_are_checked_before_any_device_work(lib):
+    """tp_poincare_trace refuses a bad face, step, length or crossing count
+    (more than 2^24 crossings per seed: rows indexed with 32-bit counts)
+    before it touches the GPU."""
+    st = C.c_int.in_dll(lib, "system_type")
+    keep = st.value
+    st.value = 4
+    f = lib.tp_poincare_trace
+    f.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p,
+                  C.c_void_p, C.c_void_p]
+    e = lib.tp_last_error
+    e.restype = C.c_char_p
+    try:
+        for args in ((1, 3, 0.5, 10.0, 4), (1, 2, 0.0, 10.0, 4), (1, 2, 0.5, -1.0, 4), (1, 2, 0.5, 10.0, 0),
+                     (1, 2, 0.5, 10.0, (1 << 24) + 1), (-1, 2, 0.5, 10.0, 4)):
+            n, face, step, length, nc = args
+            assert f(n, None, face, step, length, nc, None, None, None, None) == -1
+            assert b"bad Poincare map arguments" in e()
+    finally:
+        st.value = keep
+        lib.tp_clear_status()
+
 @pytest.mark.parametrize("case", ["no_step_label", "no_ff_label", "no_file", "no_wlcs_config"])
 def test_config_errors_exit_like_the_reference(tmp_path, case):
     """Malformed or missing configuration: a message on stdout and exit(1), as
