@@ -7,6 +7,7 @@
 // steps keep working while others take many.  The extrapolation tableau is
 // FP64.  Every loop is bounded: a per-step rejection cap and a per-particle
 // step cap end in a status code, never in a spin.
+#include <climits>
 #include <cmath>
 #include <cstring>
 
@@ -750,6 +751,10 @@ extern "C" int tp_bs_run(int n, double* y, double* t, double t_end, int nt_out, 
     if (!ensure_thresholds(nbins)) return -1;
     if (n <= 0 || nt_out < 1) {
         set_error(1, "tp_bs_run: need particles and frames");
+        return -1;
+    }
+    if ((long long)nt_out * nbins > INT_MAX) {  // the kernel indexes the spectrum with 32-bit integers
+        set_error(1, "tp_bs_run: spectra of %d frames x %d bins: not supported", nt_out, nbins);
         return -1;
     }
     size_t nspec = (size_t)nt_out * nbins;
