@@ -176,7 +176,7 @@ bool parse_type(Cur& c, Type& t, int depth = 0)
     case 6: {  // compound
         const int n = (int)(bits & 0xffff);
         int offbytes = 1;
-        while (offbytes < 8 && (size >> (8 * offbytes)) != 0) offbytes++;
+        while (offbytes < 4 && (size >> (8 * offbytes)) != 0) offbytes++;  // size is 32-bit
         t.cls = 6;
         for (int m = 0; m < n && c.ok; m++) {
             Member mb;

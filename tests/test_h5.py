@@ -532,3 +532,47 @@ def test_large_transfers_split_across_threads(lib, tmp_path):
     f = h5ref.File(fn)
     for name, a in zip(("xpos", "ypos", "zpos"), xyz):
         assert np.array_equal(f.read("/poincare_map/" + name), a)
+
+
+@pytest.mark.parametrize("layout", ["compact_v2", "chunked_shuffle_deflate"])
+def test_reader_under_sanitizers(tmp_path, layout):
+    """The reader built with AddressSanitizer and UndefinedBehaviorSanitizer
+    (tests/h5lite_fuzz.cpp) on 4,000 files, each with one or two bytes changed
+    outside the raw data: every open, description and read either succeeds or
+    is refused, with no invalid access and no undefined behaviour."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no g++")
+    exe = str(tmp_path / "fuzz")
+    r = subprocess.run([gxx, "-O1", "-g", "-std=c++17", "-fsanitize=address,undefined",
+                        "-fno-sanitize-recover=undefined", "-I", os.path.join(ROOT, "test_particle_gb300", "csrc"),
+                        "-o", exe, os.path.join(ROOT, "tests", "h5lite_fuzz.cpp"), "-ldl"],
+                       capture_output=True, text=True)
+    if r.returncode != 0 and "asan" in r.stderr.lower():
+        pytest.skip("sanitizer runtime not available")
+    assert r.returncode == 0, r.stderr[-2000:]
+    rng = np.random.default_rng(1)
+    dt = np.dtype([(k, ">f8") for k in ("x", "y", "z", "qm", "ux", "uy", "uz", "t")])
+    tree = {"top": rng.normal(size=7), "g": {"d": rng.normal(size=(4, 5, 3))},
+            "particles_fields": {"particles": np.zeros(6, dtype=dt)}}
+    kw = dict(layout="compact", layout_version=2) if layout == "compact_v2" else \
+        dict(layout="chunked", chunks={"g/d": (2, 3, 2), "top": (3,)}, filters=("shuffle", "deflate"))
+    fn = str(tmp_path / "base.h5")
+    h5ref.write(fn, tree, compound_version=1, **kw)
+    f = h5ref.File(fn)
+    mask = np.ones(os.path.getsize(fn), bool)
+    for path in ("/top", "/g/d", "/particles_fields/particles"):
+        dims, dtype, lay = f.info(path)[:3]
+        if lay[0] == "contiguous" and lay[1] != h5ref.UNDEF:
+            a = lay[1] + f.base
+            mask[a:a + int(np.prod(dims)) * dtype.itemsize] = False
+    pos = str(tmp_path / "pos.bin")
+    np.nonzero(mask)[0].astype(np.int64).tofile(pos)
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
+    r = subprocess.run([exe, fn, pos, str(tmp_path / "work.h5"), "4000", "11"], capture_output=True, text=True,
+                       timeout=600, env=env)
+    assert r.returncode == 0, (r.stdout[-500:], r.stderr[-3000:])
+    ok, refused = (int(v) for v in r.stdout.split()[1:3])
+    assert ok > 0 and refused > 0
