@@ -229,8 +229,8 @@ bool parse_type(Cur& c, Type& t, int depth = 0)
 // A datatype's encoding in the earliest format (version 1).
 void encode_atomic(std::vector<uint8_t>& o, const Atomic& a)
 {
-    auto put = [&](uint64_t v, int n) {
-        for (int i = 0; i < n; i++) o.push_back((uint8_t)(v >> (8 * i)));
+    auto put = [&](uint64_t v, int n) {  // n little-endian bytes (zeros past the eighth)
+        for (int i = 0; i < n; i++) o.push_back(i < 8 ? (uint8_t)(v >> (8 * i)) : (uint8_t)0);
     };
     if (a.cls == 1) {
         o.push_back(0x11);
@@ -262,8 +262,8 @@ void encode_type(std::vector<uint8_t>& o, const Type& t)
         encode_atomic(o, t.atom);
         return;
     }
-    auto put = [&](uint64_t v, int n) {
-        for (int i = 0; i < n; i++) o.push_back((uint8_t)(v >> (8 * i)));
+    auto put = [&](uint64_t v, int n) {  // n little-endian bytes (zeros past the eighth)
+        for (int i = 0; i < n; i++) o.push_back(i < 8 ? (uint8_t)(v >> (8 * i)) : (uint8_t)0);
     };
     o.push_back(0x16);
     put(t.members.size(), 3);
